@@ -1,0 +1,138 @@
+// Internal definitions shared by the CUDA kernels and the host side of libdtwx.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace dtwx {
+
+constexpr int kWarp = 32;
+constexpr int kKmer = 6;
+constexpr int kTableSize = 4096;
+// Rows between two running-minimum rescales of the FP16 cells.
+constexpr int kRescaleRows = 32;
+// Bounded device-side waits: iterations before a wait gives up and flags an error.
+constexpr uint32_t kSpinLimit = 1u << 26;
+
+// Task flags.
+constexpr int32_t kTaskResume = 1;    // start from the saved row state instead of free start
+constexpr int32_t kTaskSaveState = 2; // write the final DP row to the row state
+
+// One unit of DP work: a read (offline) or one chunk of a read (serving).
+// Rows are query samples query[q_off .. q_off + n); every output column of the
+// reference is covered by the work items (task, chunk) of the task.
+struct Task {
+  int64_t q_off;     // offset of the first sample in the query buffer
+  int32_t n;         // rows (samples) in this task
+  int32_t flags;     // kTaskResume | kTaskSaveState
+  int64_t state_off; // offset, in columns, of this read's row state
+  int32_t out_slot;  // result slot: keys[2*out_slot + strand]
+  int32_t pad;
+};
+static_assert(sizeof(Task) == 32, "Task layout");
+
+// Device error flags (bit mask in *err).
+constexpr int32_t kErrTmaTimeout = 1;
+constexpr int32_t kErrBadTask = 2;
+
+struct SdtwParams {
+  const float *query;          // z-scored samples, FP32
+  const Task *tasks;           // n_tasks
+  const int32_t *order;        // processing order of tasks (longest first); NULL = identity
+  unsigned long long *keys;    // 2 per out slot: (orderable score << 32) | end column
+  float2 *state;               // row-state pool (absolute FP32 values), NULL if unused
+  char *seam;                  // per-warp scratch (seam columns + epoch offsets)
+  int32_t *counter;            // work-queue ticket counter (zeroed before launch)
+  int32_t *err;                // device error flags
+  const void *ref_plain;       // ref pairs in global memory (used when TMA is off)
+  int64_t m;                   // valid columns per strand
+  int64_t m_pad;               // padded columns (multiple of the strip width)
+  int64_t seam_stride;         // bytes of scratch per warp
+  int32_t n_tasks;
+  int32_t n_chunks;            // chunks per task
+  int32_t chunk_strips;        // strips per chunk
+  int32_t max_rows;            // capacity of the seam buffers (rows)
+  int32_t n_items;             // n_tasks * n_chunks
+  int32_t use_tma;
+};
+
+// Per-warp scratch layout, in bytes, for a pair type of `pair_bytes` bytes.
+// Each half (one per strip parity) holds the seam column, (max_rows + 1)
+// pairs, then from a 16-byte aligned position the FP32 offsets of the
+// epochs, (max_rows / kRescaleRows + 2) float2.
+inline __host__ __device__ int64_t seam_offsets_pos(int pair_bytes, int max_rows) {
+  return ((int64_t)(max_rows + 1) * pair_bytes + 15) & ~(int64_t)15;
+}
+inline __host__ __device__ int64_t seam_bytes_per_warp(int pair_bytes, int max_rows) {
+  const int64_t epochs = (int64_t)(max_rows / kRescaleRows + 2) * 8;
+  int64_t per = seam_offsets_pos(pair_bytes, max_rows) + epochs;
+  per = (per + 255) & ~(int64_t)255;
+  return 2 * per;  // ping-pong between consecutive strips
+}
+
+// Orderable 32-bit image of a float: unsigned order == float order.
+__host__ __device__ inline uint32_t float_to_ordered(float f) {
+  uint32_t u;
+#ifdef __CUDA_ARCH__
+  u = __float_as_uint(f);
+#else
+  memcpy(&u, &f, 4);
+#endif
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ inline float ordered_to_float(uint32_t o) {
+  uint32_t u = (o & 0x80000000u) ? (o & 0x7fffffffu) : ~o;
+  float f;
+#ifdef __CUDA_ARCH__
+  f = __uint_as_float(u);
+#else
+  memcpy(&f, &u, 4);
+#endif
+  return f;
+}
+
+// ---------------------------------------------------------------- launchers
+// (defined in the .cu files; all return cudaError_t of the launch)
+
+// sDTW over all (task, chunk) items.  precision: 0 FP16, 1 FP32.
+// cells_per_thread must be one of the compiled instances.
+cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, int grid,
+                        const SdtwParams &p, const CUtensorMap *tmap, cudaStream_t s);
+// Dynamic shared memory the sDTW kernel needs per CTA.
+size_t sdtw_smem_bytes(int precision, int cells_per_thread, int warps_per_cta);
+// Resident CTAs per SM for the given shape (occupancy API), 0 on error.
+int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta);
+bool sdtw_instance_exists(int precision, int cells_per_thread);
+int sdtw_pair_bytes(int precision);
+
+// Reference builder: genome bytes -> z-scored (fwd, rev) pairs in FP16 and FP32.
+cudaError_t launch_build_reference(const char *d_seq, int64_t L, const double *d_table,
+                                   int64_t m, int64_t m_pad, int concat, double *d_work,
+                                   __half2 *d_ref16, float2 *d_ref32, float *d_fwd32,
+                                   float *d_rev32, cudaStream_t s);
+size_t build_reference_work_bytes(int64_t m);
+
+// Window + z-score of raw reads into the query buffer.
+// src: raw samples (float or int16 when is_i16); for read r the window starts at
+// src_off[r] and has dst_len[r] samples written to dst + dst_off[r].
+cudaError_t launch_normalize(const void *src, int is_i16, const int64_t *src_off,
+                             const int64_t *dst_off, const int32_t *dst_len,
+                             const float *scale_mul, const float *scale_add, int n_reads,
+                             float eps, float *dst, cudaStream_t s);
+
+// Keys -> dtwx_result records.
+cudaError_t launch_finalize(const unsigned long long *keys, const int32_t *n_samples,
+                            int n_reads, int concat, int64_t m_fwd, float threshold,
+                            void *d_results, cudaStream_t s);
+
+// Reset keys to the empty value and the work counter to zero.
+cudaError_t launch_reset(unsigned long long *keys, int n_keys, int32_t *counter,
+                         cudaStream_t s);
+
+// Issue-rate probe.
+cudaError_t launch_peak_probe(int precision, int grid, int block, int iters,
+                              float *sink, cudaStream_t s);
+
+}  // namespace dtwx

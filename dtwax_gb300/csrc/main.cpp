@@ -1,0 +1,274 @@
+// dtwx_main -- command-line drop-in for DTWax's `main <fast5_folder> <kmer_model> <ref.fasta>`
+// (src/main.cu:53-318).
+//
+//   dtwx_main <read_folder> <kmer_model> <ref.fasta> [options]
+//
+// Prints the reference's 6-column log on stdout (src/main.cu:289-297):
+//   Read_ID  QUERY_LEN  REF_LEN  sDTW score: fwd-strand  sDTW score: rev-strand
+//   <idx>\t<read_id>\t<QUERY_LEN>\t<REF_LEN>\t<fwd>\t<rev>
+// so src/ReadUntil/calc_classification_threshold.py and plot_realtime.py keep
+// parsing it.  Timing goes to stderr.  The best end position, strand and call
+// go to an optional side file (--side), one line per read:
+//   <idx>\t<read_id>\t<score>\t<end_pos>\t<strand: + or ->\t<call: target|non-target|skipped>
+//
+// Reads: FAST5 needs HDF5, which this build does not link, so the folder holds
+// one read per file as a 1-D numpy array (*.npy: int16 ADC or float32/float64
+// pA) or as whitespace-separated text samples (*.txt).  The read id is the file
+// name without its extension.  Files are taken in name order.
+//
+// Options:
+//   --fp32             FP32 cells (default FP16 half2 with running-min offset)
+//   --threshold T      score below T calls "target" (default 194)
+//   --adapter N        samples skipped at the read start (default 1952, ADAPTER_LEN)
+//   --query-len N      samples aligned per read (default 2048, QUERY_LEN; 0 = rest)
+//   --allow-short      align reads shorter than adapter + query-len (default: skip them)
+//   --max-ref-len N    cap k-mer positions per strand (REF_LEN compatibility)
+//   --concat           score one sequence fwd||rev instead of the two strands
+//   --side FILE        write end position, strand and call per read
+#include <dirent.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "dtwx.h"
+
+namespace {
+
+bool ends_with(const std::string &s, const std::string &suf) {
+  return s.size() >= suf.size() && s.compare(s.size() - suf.size(), suf.size(), suf) == 0;
+}
+
+// Minimal .npy reader for 1-D little-endian int16/int32/float32/float64 arrays.
+bool load_npy(const std::string &path, std::vector<float> &out, std::string &err) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) {
+    err = "cannot open";
+    return false;
+  }
+  char magic[6];
+  f.read(magic, 6);
+  if (!f || memcmp(magic, "\x93NUMPY", 6) != 0) {
+    err = "not a .npy file";
+    return false;
+  }
+  unsigned char ver[2];
+  f.read(reinterpret_cast<char *>(ver), 2);
+  uint32_t hlen = 0;
+  if (ver[0] == 1) {
+    unsigned char b[2];
+    f.read(reinterpret_cast<char *>(b), 2);
+    hlen = b[0] | (b[1] << 8);
+  } else {
+    unsigned char b[4];
+    f.read(reinterpret_cast<char *>(b), 4);
+    hlen = b[0] | (b[1] << 8) | (b[2] << 16) | ((uint32_t)b[3] << 24);
+  }
+  std::string header(hlen, '\0');
+  f.read(&header[0], hlen);
+  if (!f) {
+    err = "truncated header";
+    return false;
+  }
+  auto field = [&](const char *key) -> std::string {
+    size_t p = header.find(key);
+    if (p == std::string::npos) return "";
+    p = header.find(':', p);
+    if (p == std::string::npos) return "";
+    ++p;
+    while (p < header.size() && header[p] == ' ') ++p;
+    size_t e = p;
+    if (header[p] == '\'') {
+      e = header.find('\'', p + 1);
+      return header.substr(p + 1, e - p - 1);
+    }
+    if (header[p] == '(') {
+      e = header.find(')', p);
+      return header.substr(p + 1, e - p - 1);
+    }
+    while (e < header.size() && header[e] != ',' && header[e] != '}') ++e;
+    return header.substr(p, e - p);
+  };
+  const std::string descr = field("'descr'");
+  const std::string fortran = field("'fortran_order'");
+  const std::string shape = field("'shape'");
+  if (fortran.find("True") != std::string::npos) {
+    err = "fortran order not supported";
+    return false;
+  }
+  size_t n = 0;
+  {
+    std::string s = shape;
+    s.erase(std::remove(s.begin(), s.end(), ' '), s.end());
+    if (!s.empty() && s.back() == ',') s.pop_back();
+    if (s.find(',') != std::string::npos) {
+      err = "expected a 1-D array";
+      return false;
+    }
+    n = s.empty() ? 1 : (size_t)std::stoull(s);
+  }
+  out.resize(n);
+  auto read_as = [&](auto tag) {
+    using T = decltype(tag);
+    std::vector<T> tmp(n);
+    f.read(reinterpret_cast<char *>(tmp.data()), sizeof(T) * n);
+    for (size_t i = 0; i < n; ++i) out[i] = (float)tmp[i];
+    return (bool)f;
+  };
+  bool ok = false;
+  if (descr == "<i2")
+    ok = read_as(int16_t());
+  else if (descr == "<i4")
+    ok = read_as(int32_t());
+  else if (descr == "<f4")
+    ok = read_as(float());
+  else if (descr == "<f8")
+    ok = read_as(double());
+  else {
+    err = "unsupported dtype " + descr;
+    return false;
+  }
+  if (!ok) err = "truncated data";
+  return ok;
+}
+
+bool load_txt(const std::string &path, std::vector<float> &out, std::string &err) {
+  std::ifstream f(path);
+  if (!f) {
+    err = "cannot open";
+    return false;
+  }
+  out.clear();
+  double v;
+  while (f >> v) out.push_back((float)v);
+  if (!f.eof()) {
+    err = "non-numeric sample";
+    return false;
+  }
+  return true;
+}
+
+int usage() {
+  std::cerr << "usage: dtwx_main <read_folder> <kmer_model> <ref.fasta> [--fp32] [--threshold T]\n"
+               "       [--adapter N] [--query-len N] [--allow-short] [--max-ref-len N] [--concat] [--side FILE]\n";
+  return 2;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  if (argc < 4) return usage();
+  const std::string folder = argv[1], model = argv[2], fasta = argv[3];
+  dtwx_config cfg;
+  dtwx_config_default(&cfg);
+  cfg.adapter_skip = 1952;
+  cfg.query_len = 2048;
+  cfg.require_full = 1;
+  std::string side;
+  for (int i = 4; i < argc; ++i) {
+    const std::string a = argv[i];
+    auto next = [&](void) -> const char * {
+      if (i + 1 >= argc) {
+        std::cerr << "missing value for " << a << "\n";
+        exit(2);
+      }
+      return argv[++i];
+    };
+    if (a == "--fp32")
+      cfg.precision = DTWX_FP32;
+    else if (a == "--threshold")
+      cfg.threshold = (float)atof(next());
+    else if (a == "--adapter")
+      cfg.adapter_skip = atoi(next());
+    else if (a == "--query-len")
+      cfg.query_len = atoi(next());
+    else if (a == "--allow-short")
+      cfg.require_full = 0;
+    else if (a == "--max-ref-len")
+      cfg.max_ref_len = atoll(next());
+    else if (a == "--concat")
+      cfg.strand_mode = DTWX_STRANDS_CONCAT;
+    else if (a == "--side")
+      side = next();
+    else
+      return usage();
+  }
+
+  std::vector<std::string> files;
+  DIR *d = opendir(folder.c_str());
+  if (!d) {
+    std::cerr << "Error opening folder '" << folder << "'\n";
+    return 1;
+  }
+  while (dirent *e = readdir(d)) {
+    const std::string n = e->d_name;
+    if (ends_with(n, ".npy") || ends_with(n, ".txt") || ends_with(n, ".fast5")) files.push_back(n);
+  }
+  closedir(d);
+  std::sort(files.begin(), files.end());
+
+  std::vector<float> raw;
+  std::vector<int64_t> offsets{0};
+  std::vector<std::string> ids;
+  for (const std::string &n : files) {
+    if (ends_with(n, ".fast5")) {
+      std::cerr << "skipping " << n << ": FAST5 needs HDF5, which this build does not link\n";
+      continue;
+    }
+    std::vector<float> s;
+    std::string err;
+    const std::string path = folder + "/" + n;
+    const bool ok = ends_with(n, ".npy") ? load_npy(path, s, err) : load_txt(path, s, err);
+    if (!ok) {
+      std::cerr << "skipping " << n << ": " << err << "\n";
+      continue;
+    }
+    raw.insert(raw.end(), s.begin(), s.end());
+    offsets.push_back((int64_t)raw.size());
+    ids.push_back(n.substr(0, n.rfind('.')));
+  }
+
+  dtwx_handle *h = nullptr;
+  int rc = dtwx_create(&cfg, model.c_str(), nullptr, fasta.c_str(), &h);
+  if (rc != DTWX_OK) {
+    std::cerr << "dtwx_create failed (" << rc << "): " << dtwx_last_error(nullptr) << "\n";
+    return 1;
+  }
+  const int n_reads = (int)ids.size();
+  std::vector<dtwx_result> res(n_reads);
+  const double t0 = dtwx_now_ms();
+  rc = dtwx_classify_batch(h, raw.data(), offsets.data(), n_reads, res.data());
+  const double ms = dtwx_now_ms() - t0;
+  if (rc != DTWX_OK) {
+    std::cerr << "dtwx_classify_batch failed (" << rc << "): " << dtwx_last_error(h) << "\n";
+    dtwx_destroy(h);
+    return 1;
+  }
+  // the reference's throughput figure, hpc_helpers.hpp:93-100
+  const double qlen = cfg.query_len > 0 ? cfg.query_len : 0;
+  std::cerr << "TIMING: " << ms << " ms " << (qlen / (ms * 1e3)) * n_reads / 10 << " Mbps (classify_batch)\n";
+
+  const int64_t ref_len = dtwx_ref_len(h);
+  std::cout << "Read_ID\tQUERY_LEN\tREF_LEN\tsDTW score: fwd-strand\tsDTW score: rev-strand\n";
+  int printed = 0;
+  std::ofstream sf;
+  if (!side.empty()) sf.open(side);
+  for (int j = 0; j < n_reads; ++j) {
+    const dtwx_result &r = res[j];
+    if (sf) {
+      sf << j << "\t" << ids[j] << "\t" << r.score << "\t" << r.end_pos << "\t" << (r.strand ? '-' : '+') << "\t"
+         << (r.call < 0 ? "skipped" : (r.call ? "target" : "non-target")) << "\n";
+    }
+    if (r.call < 0) continue;  // the reference drops reads shorter than the window
+    std::cout << printed++ << "\t" << ids[j] << "\t" << r.n_samples << "\t" << ref_len << "\t" << r.score_fwd
+              << "\t" << r.score_rev << "\n";
+  }
+  dtwx_destroy(h);
+  return 0;
+}

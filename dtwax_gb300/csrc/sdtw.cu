@@ -1,0 +1,586 @@
+// sDTW kernels for sm_103a: the persistent batched kernel (FP16 half2 with a
+// running-minimum offset, or FP32) and the issue-rate probe used as roofline.
+//
+// Recurrence (src/include/DTW.cu:37-39 with -DNO_REF_DEL; scripts/sdtw.py:205-225):
+//   D[i][j] = (r_j - q_i)^2 + min(D[i-1][j], D[i-1][j-1]),   free start (row -1 = 0),
+//   D[i][0] = D[i-1][0] + (r_0 - q_i)^2,   result = min_j D[n-1][j] and its column.
+//
+// Layout of the work.  A row depends only on the previous row (there is no
+// horizontal term), so the 32 lanes of a warp sweep the SAME row together; lane
+// l owns the S consecutive columns x + l*S .. x + l*S + S-1 of a 32*S-column
+// "strip", keeps them in registers, and receives the diagonal predecessor of
+// its first column from lane l-1 by one __shfl_up_sync per row.  Lane 0 takes
+// it from the seam column written by the strip to the left.
+//
+// A work item is (task, chunk): the task's rows against output columns
+// [a, b) of the reference.  The warp sweeps the strips of [x0, b) left to right
+// (ref strip staged into shared memory by a TMA tensor copy, double buffered),
+// handing each strip's last column to the next strip through per-warp
+// scratch.  Chunks are independent: a chunk starting at a > 0 recomputes a
+// halo of >= n columns to its left, with +inf entering at the halo's left edge;
+// that error moves right one column per row, so it never reaches column a.
+// Halo strips stop at the last row that can still influence column a.
+//
+// FP16: cells are __half2 (fwd strand in .x, rev in .y).  Every kRescaleRows
+// rows each strip subtracts its own row minimum from its cells and adds it to
+// an FP32 offset, so the cells near the minimum stay small and precise.  The
+// seam value crossing into the next strip is re-based by the difference of the
+// two strips' offsets (one per epoch of kRescaleRows rows).
+#include "dtwx_internal.h"
+
+#include <cuda/std/cstdint>
+
+namespace dtwx {
+
+#define FULL_MASK 0xffffffffu
+
+// ---------------------------------------------------------------- precision policies
+
+template <int PREC> struct Pol;
+
+template <> struct Pol<0> {  // FP16 pairs
+  using V = __half2;
+  static constexpr int PB = 4;
+  __device__ __forceinline__ static V inf() { return __half2half2(__ushort_as_half((unsigned short)0x7c00u)); }
+  __device__ __forceinline__ static V zero() { return __half2half2(__ushort_as_half((unsigned short)0)); }
+  __device__ __forceinline__ static V qv(float q) { return __float2half2_rn(q); }
+  __device__ __forceinline__ static V cell(V r, V q, V a, V b) {
+    const V d = __hsub2(r, q);
+    return __hfma2(d, d, __hmin2(a, b));
+  }
+  __device__ __forceinline__ static V vmin(V a, V b) { return __hmin2(a, b); }
+  __device__ __forceinline__ static V shfl(V v, int src) { return __shfl_sync(FULL_MASK, v, src); }
+  __device__ __forceinline__ static V shfl_up(V v) { return __shfl_up_sync(FULL_MASK, v, 1); }
+  __device__ __forceinline__ static V shfl_xor(V v, int m) { return __shfl_xor_sync(FULL_MASK, v, m); }
+  __device__ __forceinline__ static float2 to_f2(V v) { return __half22float2(v); }
+  __device__ __forceinline__ static V from_f2(float2 f) { return __float22half2_rn(f); }
+  // query window: one half2 (q, q) per lane, broadcast by one shuffle per row
+  using QW = __half2;
+  __device__ __forceinline__ static QW qw(float q) { return __float2half2_rn(q); }
+  __device__ __forceinline__ static V qbcast(QW w, int il) { return __shfl_sync(FULL_MASK, w, il); }
+};
+
+template <> struct Pol<1> {  // FP32 pairs
+  using V = float2;
+  static constexpr int PB = 8;
+  __device__ __forceinline__ static V inf() { return make_float2(__int_as_float(0x7f800000), __int_as_float(0x7f800000)); }
+  __device__ __forceinline__ static V zero() { return make_float2(0.f, 0.f); }
+  __device__ __forceinline__ static V qv(float q) { return make_float2(q, q); }
+  __device__ __forceinline__ static V cell(V r, V q, V a, V b) {
+    const float dx = r.x - q.x, dy = r.y - q.y;
+    return make_float2(fmaf(dx, dx, fminf(a.x, b.x)), fmaf(dy, dy, fminf(a.y, b.y)));
+  }
+  __device__ __forceinline__ static V vmin(V a, V b) { return make_float2(fminf(a.x, b.x), fminf(a.y, b.y)); }
+  __device__ __forceinline__ static V shfl(V v, int src) {
+    return make_float2(__shfl_sync(FULL_MASK, v.x, src), __shfl_sync(FULL_MASK, v.y, src));
+  }
+  __device__ __forceinline__ static V shfl_up(V v) {
+    return make_float2(__shfl_up_sync(FULL_MASK, v.x, 1), __shfl_up_sync(FULL_MASK, v.y, 1));
+  }
+  __device__ __forceinline__ static V shfl_xor(V v, int m) {
+    return make_float2(__shfl_xor_sync(FULL_MASK, v.x, m), __shfl_xor_sync(FULL_MASK, v.y, m));
+  }
+  __device__ __forceinline__ static float2 to_f2(V v) { return v; }
+  __device__ __forceinline__ static V from_f2(float2 f) { return f; }
+  using QW = float;
+  __device__ __forceinline__ static QW qw(float q) { return q; }
+  __device__ __forceinline__ static V qbcast(QW w, int il) {
+    const float v = __shfl_sync(FULL_MASK, w, il);
+    return make_float2(v, v);
+  }
+};
+
+// ---------------------------------------------------------------- TMA / mbarrier helpers
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// Bounded wait on an mbarrier phase; false when the wait gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  const uint32_t addr = smem_u32(bar);
+  for (uint32_t it = 0; it < kSpinLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// 2-D tiled TMA load: box of the tensor map at (c0, c1) into shared memory.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0,
+                                            int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Byte offset of logical byte b of a tile written by TMA with 128-byte
+// swizzling: the 16-byte chunk index inside each 128-byte row is XOR-ed with
+// the row index modulo 8.
+__device__ __forceinline__ uint32_t swz128(uint32_t b) {
+  const uint32_t row = b >> 7;
+  const uint32_t chunk = (b >> 4) & 7u;
+  return (row << 7) | ((chunk ^ (row & 7u)) << 4) | (b & 15u);
+}
+
+// ---------------------------------------------------------------- ref strip -> registers
+
+template <int S, int PREC>
+__device__ __forceinline__ void regs_from_smem(const unsigned char *tile, int lane,
+                                               typename Pol<PREC>::V (&R)[S]) {
+  using V = typename Pol<PREC>::V;
+  constexpr int PB = Pol<PREC>::PB;
+  constexpr int PER16 = 16 / PB;  // pairs per 16-byte load
+  static_assert((S * PB) % 16 == 0, "lane slice must be 16-byte aligned");
+#pragma unroll
+  for (int k = 0; k < S; k += PER16) {
+    const uint32_t b = (uint32_t)((lane * S + k) * PB);
+    const uint4 v = *reinterpret_cast<const uint4 *>(tile + swz128(b));
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int u = 0; u < PER16; ++u) {
+      V r;
+      memcpy(&r, &w[u * (PB / 4)], PB);
+      R[k + u] = r;
+    }
+  }
+}
+
+template <int S, int PREC>
+__device__ __forceinline__ void regs_from_global(const void *ref, int64_t x, int lane,
+                                                 typename Pol<PREC>::V (&R)[S]) {
+  using V = typename Pol<PREC>::V;
+  constexpr int PB = Pol<PREC>::PB;
+  constexpr int PER16 = 16 / PB;
+  const unsigned char *base = reinterpret_cast<const unsigned char *>(ref) + (x + (int64_t)lane * S) * PB;
+#pragma unroll
+  for (int k = 0; k < S; k += PER16) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(base + k * PB));
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int u = 0; u < PER16; ++u) {
+      V r;
+      memcpy(&r, &w[u * (PB / 4)], PB);
+      R[k + u] = r;
+    }
+  }
+}
+
+// One DP row of this lane's S columns.  The previous row is in D; columns are
+// updated from right to left so D[k-1] still holds the previous row when
+// column k reads it.  The diagonal predecessor of column 0 comes from lane-1
+// (shuffle) or, on lane 0, from the seam column of the strip to the left.
+template <int S, int PREC>
+__device__ __forceinline__ void sweep_row(typename Pol<PREC>::V (&D)[S], const typename Pol<PREC>::V (&R)[S],
+                                          typename Pol<PREC>::V qq, typename Pol<PREC>::V seam, int lane) {
+  using P = Pol<PREC>;
+  const typename P::V up = P::shfl_up(D[S - 1]);
+  const typename P::V left = lane == 0 ? seam : up;
+#pragma unroll
+  for (int k = S - 1; k >= 1; --k) D[k] = P::cell(R[k], qq, D[k], D[k - 1]);
+  D[0] = P::cell(R[0], qq, D[0], left);
+}
+
+// Warp-wide lexicographic min of (value, column).
+__device__ __forceinline__ void warp_argmin(float &v, int64_t &j) {
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) {
+    const float ov = __shfl_xor_sync(FULL_MASK, v, m);
+    const int64_t oj = __shfl_xor_sync(FULL_MASK, j, m);
+    if (ov < v || (ov == v && (uint64_t)oj < (uint64_t)j)) {
+      v = ov;
+      j = oj;
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned long long make_key(float v, int64_t j) {
+  return ((unsigned long long)float_to_ordered(v) << 32) | (unsigned long long)(uint32_t)j;
+}
+
+// ---------------------------------------------------------------- the persistent kernel
+
+// Register cap per instance: the S cells and S reference pairs of a lane plus
+// about 40 registers of bookkeeping, rounded to 128 or 168 (16 or 12 warps/SM).
+template <int S, int PREC>
+constexpr int sdtw_reg_cap() { return (S * Pol<PREC>::PB / 4) * 2 + 40 <= 128 ? 128 : 168; }
+
+template <int S, int PREC>
+__global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                   const SdtwParams p) {
+  using P = Pol<PREC>;
+  using V = typename P::V;
+  constexpr int W = kWarp * S;                // columns per strip
+  constexpr int PB = P::PB;
+  constexpr int STRIP_BYTES = W * PB;
+  constexpr int K = kRescaleRows;
+  static_assert(STRIP_BYTES % 1024 == 0, "strip tile must keep 1024-byte alignment");
+  static_assert(S % 2 == 0, "row state is moved as float4 pairs of columns");
+
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  unsigned char *const slot0 = smem + (2 * warp) * STRIP_BYTES;  // slot s at slot0 + s*STRIP_BYTES
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * nwarps * STRIP_BYTES) + 2 * warp;
+
+  if (p.use_tma && lane == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  uint32_t phase = 0;  // bit s = parity of the next completion of slot s
+
+  const int64_t gwarp = (int64_t)blockIdx.x * nwarps + warp;
+  char *seam_base = p.seam + gwarp * p.seam_stride;
+  const int64_t seam_half = p.seam_stride / 2;
+  const int64_t off_pos = seam_offsets_pos(PB, p.max_rows);
+  const int64_t C = (int64_t)p.chunk_strips * W;
+
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(p.counter, 1);
+    item = __shfl_sync(FULL_MASK, item, 0);
+    if (item >= p.n_items) break;
+    const int tr = item / p.n_chunks;
+    const int chunk = item - tr * p.n_chunks;
+    const int ti = p.order ? p.order[tr] : tr;
+    const Task t = p.tasks[ti];
+    const int n = t.n;
+    if (n <= 0 || n > p.max_rows) {
+      if (n > p.max_rows && lane == 0) atomicOr(p.err, kErrBadTask);
+      continue;
+    }
+    const int64_t a = (int64_t)chunk * C;
+    const int64_t b = min(a + C, p.m);
+    int64_t x0 = 0;
+    if (chunk > 0) {
+      const int64_t halo = ((int64_t)n + W - 1) / W * W;
+      x0 = a - halo > 0 ? a - halo : 0;
+    }
+    const int nstrips = (int)((b - x0 + W - 1) / W);
+    const float *q = p.query + t.q_off;
+    const bool resume = (t.flags & kTaskResume) != 0;
+    const bool save = (t.flags & kTaskSaveState) != 0 && p.state != nullptr;
+
+    float bestx = __int_as_float(0x7f800000), besty = bestx;
+    int64_t colx = -1, coly = -1;
+
+    if (p.use_tma && lane == 0) {
+      mbar_expect_tx(&bars[0], STRIP_BYTES);
+      fence_proxy_async_smem();
+      tma_load_2d(slot0, &tmap, &bars[0], 0, (int)(x0 * PB / 128));
+    }
+
+    for (int s = 0; s < nstrips; ++s) {
+      const int64_t x = x0 + (int64_t)s * W;
+      const bool relevant = x >= a;
+      const bool first = (s == 0);
+      int rows = n;
+      if (!relevant) {
+        const int64_t lim = (int64_t)n - 1 - (a - x - W);
+        rows = (int)(lim < 0 ? 0 : (lim > n ? n : lim));
+      }
+
+      // -- seam buffers (ping-pong by strip parity)
+      char *in_b = seam_base + ((s + 1) & 1) * seam_half;
+      char *out_b = seam_base + (s & 1) * seam_half;
+      const V *seam_in = reinterpret_cast<const V *>(in_b);
+      const float2 *off_in = reinterpret_cast<const float2 *>(in_b + off_pos);
+      V *seam_out = reinterpret_cast<V *>(out_b);
+      float2 *off_out = reinterpret_cast<float2 *>(out_b + off_pos);
+
+      // -- initial row ("row -1"): zeros (free start) or the saved row state
+      V D[S];
+      float2 O = make_float2(0.f, 0.f);
+      if (resume) {
+        // two passes over the saved row: strip minimum first (FP16 frame), then the cells
+        const float4 *st = reinterpret_cast<const float4 *>(p.state + t.state_off + x + (int64_t)lane * S);
+        if constexpr (PREC == 0) {
+          float mx = __int_as_float(0x7f800000), my = mx;
+#pragma unroll
+          for (int k = 0; k < S / 2; ++k) {
+            const float4 v = st[k];
+            mx = fminf(mx, fminf(v.x, v.z));
+            my = fminf(my, fminf(v.y, v.w));
+          }
+#pragma unroll
+          for (int m = 16; m >= 1; m >>= 1) {
+            mx = fminf(mx, __shfl_xor_sync(FULL_MASK, mx, m));
+            my = fminf(my, __shfl_xor_sync(FULL_MASK, my, m));
+          }
+          O = make_float2(mx, my);
+        }
+#pragma unroll
+        for (int k = 0; k < S / 2; ++k) {
+          const float4 v = st[k];
+          D[2 * k] = P::from_f2(make_float2(v.x - O.x, v.y - O.y));
+          D[2 * k + 1] = P::from_f2(make_float2(v.z - O.x, v.w - O.y));
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < S; ++k) D[k] = P::zero();
+      }
+      // -- reference strip into registers (after the row state: fewer live registers)
+      V R[S];
+      if (p.use_tma) {
+        const int sl = s & 1;
+        // every lane waits (acquire of the TMA bytes); the give-up decision is warp-uniform
+        const bool ok = __all_sync(FULL_MASK, mbar_wait(&bars[sl], (phase >> sl) & 1u));
+        if (!ok) {
+          if (lane == 0) atomicOr(p.err, kErrTmaTimeout);
+          return;
+        }
+        phase ^= 1u << sl;
+        regs_from_smem<S, PREC>(slot0 + sl * STRIP_BYTES, lane, R);
+        __syncwarp();
+        if (s + 1 < nstrips && lane == 0) {
+          const int ns = (s + 1) & 1;
+          fence_proxy_async_smem();
+          mbar_expect_tx(&bars[ns], STRIP_BYTES);
+          tma_load_2d(slot0 + ns * STRIP_BYTES, &tmap, &bars[ns], 0, (int)((x + W) * PB / 128));
+        }
+      } else {
+        regs_from_global<S, PREC>(p.ref_plain, x, lane, R);
+      }
+
+      if (lane == 31) seam_out[0] = D[S - 1];
+      if constexpr (PREC == 0) {
+        if (lane == 0) off_out[0] = O;
+      }
+
+      // offset of this strip's frame relative to the left strip's frame
+      V delta = P::zero();
+      float2 off_next = make_float2(0.f, 0.f);
+      if constexpr (PREC == 0) {
+        if (!first) {
+          const float2 oi = off_in[0];
+          delta = P::from_f2(make_float2(oi.x - O.x, oi.y - O.y));
+          if (n >= K) off_next = off_in[1];
+        }
+      }
+
+      // -- row sweep, 32 rows per window: lane l holds query sample i0+l and
+      // the incoming seam value of row i0+l, already re-based into this strip's
+      // frame (delta changes only at a rescale, which ends a window)
+      const V vinf = P::inf();
+      typename P::QW qwin = P::qw(lane < n ? q[lane] : 0.f);
+      V swin = (!first && lane < rows) ? seam_in[lane] : vinf;
+      if constexpr (PREC == 0) swin = __hadd2(swin, delta);
+      V *so = seam_out + 1;  // seam value of row i goes to seam_out[i + 1]
+      for (int i0 = 0; i0 < rows; i0 += kWarp) {
+        const int r = i0 + kWarp + lane;
+        const float qn = r < n ? q[r] : 0.f;
+        const V sn = (!first && r < rows) ? seam_in[r] : vinf;
+        if (rows - i0 >= kWarp) {
+#pragma unroll 4
+          for (int il = 0; il < kWarp; ++il) {
+            sweep_row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), lane);
+            if (lane == 31) so[il] = D[S - 1];
+          }
+          if constexpr (PREC == 0) {
+            // rescale: subtract this strip's row minimum (one epoch = 32 rows)
+            V mn = D[0];
+#pragma unroll
+            for (int k = 1; k < S; ++k) mn = __hmin2(mn, D[k]);
+#pragma unroll
+            for (int m = 16; m >= 1; m >>= 1) mn = __hmin2(mn, P::shfl_xor(mn, m));
+#pragma unroll
+            for (int k = 0; k < S; ++k) D[k] = __hsub2(D[k], mn);
+            const float2 mf = __half22float2(mn);
+            O.x += mf.x;
+            O.y += mf.y;
+            const int e = (i0 + kWarp) / K;
+            if (lane == 0) off_out[e] = O;
+            if (lane == 31) so[kWarp - 1] = D[S - 1];  // the seam leaves in the new frame
+            if (!first) {
+              delta = P::from_f2(make_float2(off_next.x - O.x, off_next.y - O.y));
+              if ((e + 1) * K <= n) off_next = off_in[e + 1];
+            }
+          }
+        } else {
+          for (int il = 0; il < rows - i0; ++il) {
+            sweep_row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), lane);
+            if (lane == 31) so[il] = D[S - 1];
+          }
+        }
+        so += kWarp;
+        qwin = P::qw(qn);
+        swin = sn;
+        if constexpr (PREC == 0) swin = __hadd2(swin, delta);
+      }
+      if (rows < n) {
+        // rows this halo strip skipped can no longer reach column a: keep them inert
+        for (int r = rows + 1 + lane; r <= n; r += kWarp) seam_out[r] = vinf;
+        if constexpr (PREC == 0) {
+          for (int e = rows / K + 1 + lane; e <= n / K; e += kWarp) off_out[e] = O;
+        }
+      }
+      __syncwarp();
+
+      if (relevant) {
+        const int64_t c0 = x + (int64_t)lane * S;
+#pragma unroll
+        for (int k = 0; k < S; ++k) {
+          const float2 v = P::to_f2(D[k]);
+          const float vx = v.x + O.x, vy = v.y + O.y;
+          const int64_t col = c0 + k;
+          if (col < b) {
+            if (vx < bestx) { bestx = vx; colx = col; }
+            if (vy < besty) { besty = vy; coly = col; }
+          }
+        }
+        if (save) {
+          float2 *st = p.state + t.state_off + c0;
+#pragma unroll
+          for (int k = 0; k < S; k += 2) {
+            const float2 v0 = P::to_f2(D[k]);
+            const float2 v1 = P::to_f2(D[k + 1]);
+            *reinterpret_cast<float4 *>(st + k) =
+                make_float4(v0.x + O.x, v0.y + O.y, v1.x + O.x, v1.y + O.y);
+          }
+        }
+      }
+    }
+
+    warp_argmin(bestx, colx);
+    warp_argmin(besty, coly);
+    if (lane == 0) {
+      if (colx >= 0) atomicMin(&p.keys[2 * (int64_t)t.out_slot + 0], make_key(bestx, colx));
+      if (coly >= 0) atomicMin(&p.keys[2 * (int64_t)t.out_slot + 1], make_key(besty, coly));
+    }
+  }
+}
+
+// ---------------------------------------------------------------- instances / launch
+
+template <int S, int PREC>
+static cudaError_t launch_inst(int warps, int grid, const SdtwParams &p, const CUtensorMap *tmap,
+                               cudaStream_t s) {
+  const size_t smem = sdtw_smem_bytes(PREC, S, warps);
+  auto fn = sdtw_kernel<S, PREC>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  CUtensorMap dummy;
+  if (!tmap) {
+    memset(&dummy, 0, sizeof(dummy));
+    tmap = &dummy;
+  }
+  fn<<<grid, warps * kWarp, smem, s>>>(*tmap, p);
+  return cudaGetLastError();
+}
+
+template <int S, int PREC>
+static int occ_inst(int warps) {
+  int n = 0;
+  const size_t smem = sdtw_smem_bytes(PREC, S, warps);
+  auto fn = sdtw_kernel<S, PREC>;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, warps * kWarp, smem) != cudaSuccess) return 0;
+  return n;
+}
+
+int sdtw_pair_bytes(int precision) { return precision == 0 ? 4 : 8; }
+
+size_t sdtw_smem_bytes(int precision, int cells_per_thread, int warps_per_cta) {
+  const size_t strip = (size_t)kWarp * cells_per_thread * sdtw_pair_bytes(precision);
+  return 1024 /* alignment slack */ + 2 * warps_per_cta * strip + 16 * warps_per_cta;
+}
+
+bool sdtw_instance_exists(int precision, int S) {
+  if (precision == 0) return S == 32 || S == 48;
+  return S == 16 || S == 24;
+}
+
+#define DTWX_DISPATCH(PREC, S, CALL) \
+  if (precision == PREC && cells_per_thread == S) return CALL<S, PREC>
+
+cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, int grid,
+                        const SdtwParams &p, const CUtensorMap *tmap, cudaStream_t s) {
+  DTWX_DISPATCH(0, 32, launch_inst)(warps_per_cta, grid, p, tmap, s);
+  DTWX_DISPATCH(0, 48, launch_inst)(warps_per_cta, grid, p, tmap, s);
+  DTWX_DISPATCH(1, 16, launch_inst)(warps_per_cta, grid, p, tmap, s);
+  DTWX_DISPATCH(1, 24, launch_inst)(warps_per_cta, grid, p, tmap, s);
+  return cudaErrorInvalidValue;
+}
+
+int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta) {
+  DTWX_DISPATCH(0, 32, occ_inst)(warps_per_cta);
+  DTWX_DISPATCH(0, 48, occ_inst)(warps_per_cta);
+  DTWX_DISPATCH(1, 16, occ_inst)(warps_per_cta);
+  DTWX_DISPATCH(1, 24, occ_inst)(warps_per_cta);
+  return 0;
+}
+
+// ---------------------------------------------------------------- issue-rate probe
+// Runs only the cell update of the sweep (sub, min, fma over a register row of
+// 32 pairs, next row from the previous one) with no shuffles, seams or memory:
+// the instruction-issue ceiling of the recurrence on this device.
+
+template <int PREC>
+__global__ void __launch_bounds__(256) peak_probe_kernel(int iters, float *sink) {
+  using P = Pol<PREC>;
+  using V = typename P::V;
+  constexpr int S = 32;
+  V R[S], D[S];
+  const float t = (float)(threadIdx.x & 7) * 0.01f;
+#pragma unroll
+  for (int k = 0; k < S; ++k) {
+    R[k] = P::qv(t + 0.03f * k);
+    D[k] = P::zero();
+  }
+  float qf = 0.25f + t;
+  for (int it = 0; it < iters; ++it) {
+    const V qq = P::qv(qf);
+#pragma unroll
+    for (int k = S - 1; k >= 1; --k) D[k] = P::cell(R[k], qq, D[k], D[k - 1]);
+    D[0] = P::cell(R[0], qq, D[0], D[S - 1]);
+    qf = -qf;
+  }
+  V acc = D[0];
+#pragma unroll
+  for (int k = 1; k < S; ++k) acc = P::vmin(acc, D[k]);
+  const float2 f = P::to_f2(acc);
+  if (f.x == 12345.678f) sink[threadIdx.x] = f.y;  // keeps the loop alive
+}
+
+cudaError_t launch_peak_probe(int precision, int grid, int block, int iters, float *sink,
+                              cudaStream_t s) {
+  if (precision == 0)
+    peak_probe_kernel<0><<<grid, block, 0, s>>>(iters, sink);
+  else
+    peak_probe_kernel<1><<<grid, block, 0, s>>>(iters, sink);
+  return cudaGetLastError();
+}
+
+}  // namespace dtwx

@@ -1,0 +1,250 @@
+/*
+ * dtwx.h -- C ABI of the GB300 subsequence-DTW (sDTW) nanopore read classifier.
+ *
+ * Drop-in for the sDTW call of DTWax (harisankarsadasivan/DTWax).  Each entry
+ * point names the reference interface it replaces (paths are inside that
+ * project).  Conventions:
+ *   - every call returns DTWX_OK (0) or a negative DTWX_E* status; the text of
+ *     the last failure is available from dtwx_last_error(handle) (the reference
+ *     prints and calls exit(), src/include/hpc_helpers.hpp:103-113);
+ *   - host pointers are borrowed for the duration of the call only; device
+ *     state (reference squiggle, scratch, serving row state) is owned by the
+ *     handle;
+ *   - one handle is driven by one host thread at a time; separate handles are
+ *     independent;
+ *   - nothing here falls back to a CPU implementation: without a usable CUDA
+ *     device dtwx_create fails with DTWX_E_CUDA.
+ */
+#ifndef DTWX_H
+#define DTWX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DTWX_ABI_VERSION 1
+
+/* status codes */
+#define DTWX_OK 0
+#define DTWX_E_ARG (-1)      /* invalid argument */
+#define DTWX_E_IO (-2)       /* file could not be read */
+#define DTWX_E_FORMAT (-3)   /* FASTA / k-mer model / input format error */
+#define DTWX_E_CUDA (-4)     /* CUDA runtime or driver error */
+#define DTWX_E_NOMEM (-5)    /* device or host allocation failed */
+#define DTWX_E_TIMEOUT (-6)  /* a bounded device-side wait gave up */
+#define DTWX_E_CAPACITY (-7) /* request exceeds a configured capacity */
+#define DTWX_E_STATE (-8)    /* call not valid in the handle's current state */
+
+/* arithmetic of the DP */
+#define DTWX_FP16 0 /* half2 (fwd, rev) cells, per-strip running-min offset kept in FP32 */
+#define DTWX_FP32 1 /* float2 (fwd, rev) cells */
+
+/* how the two strands are scored */
+#define DTWX_STRANDS_PAIRED 0 /* fwd and rev aligned separately (DTW.cu half2 .x/.y) */
+#define DTWX_STRANDS_CONCAT 1 /* one sequence fwd||rev (load_reference.hpp:36-37, sdtw.py:234) */
+
+typedef struct dtwx_config {
+  int32_t abi_version;     /* DTWX_ABI_VERSION */
+  int32_t precision;       /* DTWX_FP16 (default) or DTWX_FP32 */
+  int32_t strand_mode;     /* DTWX_STRANDS_PAIRED (default) or DTWX_STRANDS_CONCAT */
+  int32_t device;          /* CUDA device ordinal */
+  int64_t max_ref_len;     /* cap on k-mer positions per strand, 0 = none
+                              (REF_LEN of src/include/common.hpp:70-74) */
+  int32_t adapter_skip;    /* samples dropped at the read start (ADAPTER_LEN, 1952 in
+                              the reference; 0 for the synthetic squiggles) */
+  int32_t query_len;       /* samples aligned per read after the skip (QUERY_LEN,
+                              2048 in the reference); 0 = the rest of the read */
+  int32_t require_full;    /* 1: reads shorter than adapter_skip + query_len are
+                              skipped, as generate_load_squiggle.hpp:412-430 does */
+  float norm_eps;          /* z-score epsilon (normalizer.cu:399 uses 1e-4) */
+  float threshold;         /* call = target when score < threshold
+                              (calc_classification_threshold.py:52) */
+  int32_t max_batch_reads; /* capacity hint for one classify call, 0 = grow on demand */
+  int32_t cells_per_thread;/* DP columns per lane; 0 = autotune */
+  int32_t chunk_strips;    /* strips (32 lanes x cells_per_thread columns) per work item; 0 = autotune */
+  int32_t warps_per_cta;   /* 0 = autotune */
+  int32_t reserved[8];
+} dtwx_config;
+
+/* Per-read outcome.  end_pos is the DP column (0-based k-mer position on the
+ * chosen strand's own 5'->3' axis) where the best alignment ends; score is
+ * min(score_fwd, score_rev) with ties going to the smaller end column, then to
+ * the forward strand.  n_samples = 0 marks a read that was skipped. */
+typedef struct dtwx_result {
+  float score;
+  float score_fwd;
+  float score_rev;
+  int32_t strand; /* 0 forward, 1 reverse complement */
+  int64_t end_pos;
+  int32_t call;   /* 1 target, 0 non-target, -1 skipped */
+  int32_t n_samples;
+} dtwx_result;
+
+typedef struct dtwx_handle dtwx_handle;
+
+/* Fill *cfg with the defaults above.  No reference counterpart (the reference
+ * uses compile-time macros, src/include/common.hpp:60-98). */
+int dtwx_config_default(dtwx_config *cfg);
+
+/* Build a classifier for one target genome.
+ * Replaces load_reference::ref_loader + read_kmer_model + load_ref_coeffs
+ * (src/include/load_reference.hpp:131-212) and the host tile re-layout of
+ * src/main.cu:93-119.  Exactly one of kmer_model_path (text "KMER mean stdev"
+ * per line) and level_table (4096 means by 2-bit code, A<C<G<T, first base most
+ * significant) is non-NULL.  The squiggle of both strands is built and
+ * z-scored on the GPU. */
+int dtwx_create(const dtwx_config *cfg, const char *kmer_model_path,
+                const float *level_table, const char *fasta_path,
+                dtwx_handle **out);
+
+/* Parse a FASTA file with the rules of load_reference::ref_loader
+ * (src/include/load_reference.hpp:164-212): a '>' line or an empty line ends
+ * the open record, a sequence line holding a space invalidates it, and only the
+ * record still open at the end of the file is kept (so the last record wins).
+ * Writes up to `cap` bases to seq_out (may be NULL to query the length) and the
+ * full length to *len_out.  Host only; needs no GPU. */
+int dtwx_load_fasta(const char *fasta_path, char *seq_out, int64_t cap, int64_t *len_out);
+
+/* Parse a k-mer model text file ("KMER mean stdev" per line; read_kmer_model,
+ * src/include/load_reference.hpp:131-161) into table_out[4096] by 2-bit code.
+ * Host only; needs no GPU. */
+int dtwx_load_kmer_model(const char *path, float *table_out);
+
+/* Same, from an in-memory base sequence (no FASTA parsing). */
+int dtwx_create_from_sequence(const dtwx_config *cfg, const float *level_table,
+                              const char *seq, int64_t seq_len,
+                              dtwx_handle **out);
+
+int dtwx_destroy(dtwx_handle *h);
+
+/* Text of the last failure on this handle (never NULL).  With h == NULL it
+ * reports the last failure of dtwx_create*. */
+const char *dtwx_last_error(const dtwx_handle *h);
+
+/* k-mer positions per strand of the loaded reference. */
+int64_t dtwx_ref_len(const dtwx_handle *h);
+
+/* Copy the z-scored squiggle (FP32, one strand each) to host arrays of
+ * dtwx_ref_len() floats.  For checking the reference builder. */
+int dtwx_get_reference(dtwx_handle *h, float *fwd, float *rev);
+
+/* Classify reads given as raw FP32 samples on the host: read r is
+ * raw[offsets[r] .. offsets[r+1]).  Window, z-score (FP64 statistics),
+ * sDTW of both strands and the min/argmin all run on the GPU; out[n_reads] is
+ * written on return.  Replaces the batch loop of src/main.cu:217-271
+ * (normalizer::normalize, src/include/normalizer.cu:370-413, then
+ * FullDTW::distances per 10-read batch). */
+int dtwx_classify_batch(dtwx_handle *h, const float *raw, const int64_t *offsets,
+                        int32_t n_reads, dtwx_result *out);
+
+/* Same for int16 ADC samples; pA = (raw + offset) * range / digitisation per
+ * read (fast5/nanopolish_fast5_io.cpp:279-315).  scale arrays may be NULL
+ * (raw used as is). */
+int dtwx_classify_batch_i16(dtwx_handle *h, const int16_t *raw, const int64_t *offsets,
+                            int32_t n_reads, const float *offset, const float *range,
+                            const float *digitisation, dtwx_result *out);
+
+/* Device-pointer entry, the in-process launcher of the reference:
+ * FullDTW::distances(ref, query, dists, num_entries, thresh, stream,
+ * device_last_row) (src/include/DTW.hpp:287-295).  d_query holds z-scored
+ * FP32 samples on the device, read r = d_query[offsets[r] .. offsets[r+1])
+ * (offsets on the HOST); d_out (device, n_reads entries) receives the results.
+ * Work is enqueued on `stream` (a cudaStream_t, NULL = the handle's stream)
+ * and the call returns without synchronising.  Scratch (work queue, seam
+ * columns, keys) is owned by the handle. */
+int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets,
+                   int32_t n_reads, dtwx_result *d_out, void *stream);
+
+/* Device-resident variant of dtwx_classify_batch: raw FP32 samples already on
+ * the device (d_raw, offsets on the host), results to d_out on `stream`.
+ * Runs the window + z-score kernel, the sDTW kernel and the finalize kernel. */
+int dtwx_classify_device(dtwx_handle *h, const float *d_raw, const int64_t *offsets,
+                         int32_t n_reads, dtwx_result *d_out, void *stream);
+
+/* One read per launch in FP32 (no persistent queue, no graph): the plain
+ * comparator the batched path is measured against.  Host buffers. */
+int dtwx_classify_plain_fp32(dtwx_handle *h, const float *raw, const int64_t *offsets,
+                             int32_t n_reads, dtwx_result *out);
+
+/* Kernel launches issued by the most recent classify/distances call. */
+int32_t dtwx_last_launch_count(const dtwx_handle *h);
+
+/* The tuned launch shape in use for the handle's precision. */
+int dtwx_get_tuning(const dtwx_handle *h, int32_t *cells_per_thread,
+                    int32_t *chunk_strips, int32_t *warps_per_cta);
+
+/* Measured issue-rate ceiling of the cell update on this device: a kernel that
+ * runs only the per-cell instruction mix (sub, min, fma) of the given
+ * precision over register-resident cells for `ms_target` milliseconds.
+ * Returns cells/s in *cells_per_s.  No reference counterpart (roofline). */
+int dtwx_peak_probe(int32_t device, int32_t precision, float ms_target, double *cells_per_s);
+
+/* ----------------------------------------------------------------- serving
+ * Read Until: per-channel signal chunks arrive as the sequencer produces
+ * them; each read's last DP row stays on the device between chunks and the
+ * sDTW resumes from it.  Replaces the FIFO loop of src/ru_main.cu:172-326 and
+ * the byte-pipe protocol of src/ReadUntil/ont_readuntil.py:29-59.  Reads are
+ * admitted while the device row-state pool has room; the rest wait. */
+typedef struct dtwx_decision {
+  int32_t channel;
+  int32_t decided;   /* 1 final (target or max chunks reached), 0 interim */
+  uint64_t read_number;
+  float score;
+  int32_t strand;
+  int32_t call;      /* 1 target, 0 non-target */
+  int64_t end_pos;
+  int32_t chunks;    /* chunks aligned so far */
+  int32_t samples;   /* samples aligned so far */
+  double latency_ms; /* last needed chunk arrival -> decision */
+} dtwx_decision;
+
+typedef struct dtwx_stats {
+  int64_t chunks_submitted;
+  int64_t chunks_processed;
+  int64_t reads_decided;
+  int64_t reads_deferred;    /* reads that waited for row-state memory */
+  int32_t queue_depth;       /* chunks waiting now */
+  int32_t in_flight;         /* reads holding row state */
+  int32_t max_in_flight;     /* row-state slots */
+  int32_t batches;           /* device batches launched */
+  double p50_latency_ms;
+  double p99_latency_ms;
+  double mean_batch_reads;
+  double state_bytes;        /* device bytes of the row-state pool */
+} dtwx_stats;
+
+/* Prepare the handle for serving.  max_in_flight = reads holding device row
+ * state at once (0: as many as state_budget_bytes allows); chunks_per_decision
+ * = chunks after which a read is decided even if not a target (the reference
+ * decides on one fixed window). */
+int dtwx_serve_start(dtwx_handle *h, int32_t max_in_flight, double state_budget_bytes,
+                     int32_t chunks_per_decision);
+
+/* Queue one chunk (FP32 pA samples) of read `read_number` on `channel`.
+ * arrival_ms is the caller's clock at arrival (for latency); < 0 = now. */
+int dtwx_submit_chunk(dtwx_handle *h, int32_t channel, uint64_t read_number,
+                      const float *samples, int32_t n, int32_t is_last, double arrival_ms);
+
+/* Launch one continuous-batching step if any chunk is ready (non-blocking when
+ * the previous step is still running); returns the chunks launched (>= 0) or a
+ * status. */
+int dtwx_serve_step(dtwx_handle *h);
+
+/* Collect decisions made so far (up to cap); returns the count. */
+int dtwx_poll_decisions(dtwx_handle *h, dtwx_decision *out, int32_t cap);
+
+/* Wait until every submitted chunk has been processed. */
+int dtwx_serve_drain(dtwx_handle *h);
+
+int dtwx_stats_get(dtwx_handle *h, dtwx_stats *out);
+
+/* Host clock in ms used for latency bookkeeping (CLOCK_MONOTONIC). */
+double dtwx_now_ms(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DTWX_H */

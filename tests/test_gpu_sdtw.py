@@ -1,0 +1,276 @@
+"""Parity of the CUDA path with the FP64 oracle, through the C ABI.
+
+Tolerances (spec precision targets): FP32 scores within 1e-5 relative
+of the FP64 oracle with the same end column; FP16 (half2 cells with the
+per-strip running-minimum offset) within 1e-2 relative.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, write_kat_files
+from gpu_util import make_classifier, oracle_classify, reads_of_lengths, small_genome
+from dtwax_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+FP32_RTOL = 1e-5
+FP16_RTOL = 1e-2
+
+
+@pytest.fixture(scope="module")
+def lib(built_lib):
+    return built_lib
+
+
+@pytest.fixture(scope="module")
+def genome_pair():
+    return small_genome(20_000, 11), small_genome(20_000, 12)
+
+
+def check_fp32(res, ora, rtol=FP32_RTOL, ends=True):
+    sf, ef, sr, er = ora
+    np.testing.assert_allclose(res["score_fwd"], sf, rtol=rtol)
+    np.testing.assert_allclose(res["score_rev"], sr, rtol=rtol)
+    if ends:
+        ok = res["n_samples"] > 0
+        # end columns must match except where the oracle itself has a near tie
+        mism = ok & ((res["strand"] == 0) & (res["end_pos"] != ef) | (res["strand"] == 1) & (res["end_pos"] != er))
+        assert mism.sum() == 0, np.nonzero(mism)
+
+
+def test_reference_builder_matches_oracle(lib, oracle):
+    g = small_genome(30_011, 3)
+    tab = synth.level_table()
+    with make_classifier(g, tab, precision=1) as clf:
+        fwd, rev = clf.reference()
+    of, orv = oracle.build_levels(g, tab.astype(np.float64))
+    assert fwd.size == len(g) - 5
+    np.testing.assert_allclose(fwd, of, rtol=0, atol=2e-6)
+    np.testing.assert_allclose(rev, orv, rtol=0, atol=2e-6)
+
+
+def test_reference_builder_nonacgt_and_cap(lib, oracle):
+    g = bytearray(small_genome(5_000, 4))
+    g[100:103] = b"NNN"
+    g[2000] = ord("a")
+    g = bytes(g)
+    tab = synth.level_table()
+    with make_classifier(g, tab, precision=1, max_ref_len=3000) as clf:
+        fwd, rev = clf.reference()
+    of, orv = oracle.build_levels(g, tab.astype(np.float64), cap=3000)
+    assert fwd.size == 3000
+    np.testing.assert_allclose(fwd, of, atol=2e-6)
+    np.testing.assert_allclose(rev, orv, atol=2e-6)
+
+
+@pytest.mark.parametrize("precision,rtol", [(1, 1e-5), (0, 1e-2)])
+def test_kat_lambda_on_gpu(lib, kat, tmp_path, precision, rtol):
+    """scripts/log on the GPU: the 4096 golden query samples against the
+    lambda fwd||rev reference cut to 48,128 k-mers per strand."""
+    import torch
+    import dtwax_gb300 as d
+    fasta, model = write_kat_files(kat, str(tmp_path))
+    with d.Classifier(fasta=fasta, kmer_model=model, precision=precision, strand_mode=d.STRANDS_CONCAT,
+                      max_ref_len=48128) as clf:
+        q = torch.tensor(kat["query"].astype(np.float32), device="cuda")
+        out = torch.zeros(32, dtype=torch.uint8, device="cuda")
+        clf.distances(q.data_ptr(), np.array([0, q.numel()]), out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        res = np.frombuffer(out.cpu().numpy().tobytes(), d.RESULT_DTYPE)
+    assert res["score"][0] == pytest.approx(float(kat["min_score"]), rel=rtol)
+    if precision == 1:
+        assert res["end_pos"][0] == 33305 and res["strand"][0] == 0
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_classify_matches_oracle(lib, oracle, genome_pair, precision):
+    g, o = genome_pair
+    tab = synth.level_table()
+    lengths = [2000, 1, 2, 31, 32, 33, 63, 64, 65, 100, 500, 1023, 1024, 1025, 1500, 2000, 2047, 2049, 3000, 777]
+    reads = reads_of_lengths(g, o, tab, lengths)
+    with make_classifier(g, tab, precision=precision) as clf:
+        res = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        ora = oracle_classify(oracle, clf, reads.raw, reads.offsets)
+    assert (res["n_samples"] == np.array(lengths)).all()
+    if precision == 1:
+        check_fp32(res, ora)
+    else:
+        sf, ef, sr, er = ora
+        np.testing.assert_allclose(res["score_fwd"], sf, rtol=FP16_RTOL, atol=1e-2)
+        np.testing.assert_allclose(res["score_rev"], sr, rtol=FP16_RTOL, atol=1e-2)
+        # targets (even indices, >= 500 samples) must end where the oracle ends
+        for i, n in enumerate(lengths):
+            if i % 2 == 0 and n >= 500:
+                best_end = ef[i] if sf[i] <= sr[i] else er[i]
+                assert abs(int(res["end_pos"][i]) - int(best_end)) <= 1
+
+
+@pytest.mark.parametrize("cells,strips,warps", [(16, 1, 8), (16, 3, 2), (24, 2, 4), (24, 50, 1)])
+def test_fp32_chunking_is_exact(lib, genome_pair, cells, strips, warps):
+    """Chunks recompute a halo, so any chunk size gives the same FP32 bits."""
+    g, o = genome_pair
+    tab = synth.level_table()
+    reads = reads_of_lengths(g, o, tab, [1500, 2000, 700, 2500, 90])
+    with make_classifier(g, tab, precision=1) as clf:
+        base = clf.classify(raw=reads.raw, offsets=reads.offsets)
+    with make_classifier(g, tab, precision=1, cells_per_thread=cells, chunk_strips=strips,
+                         warps_per_cta=warps) as clf:
+        res = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        t = clf.tuning()
+    assert t["cells_per_thread"] == cells and t["chunk_strips"] == strips
+    np.testing.assert_array_equal(res["score_fwd"], base["score_fwd"])
+    np.testing.assert_array_equal(res["score_rev"], base["score_rev"])
+    np.testing.assert_array_equal(res["end_pos"], base["end_pos"])
+
+
+@pytest.mark.parametrize("cells,strips", [(32, 1), (48, 2), (32, 7)])
+def test_fp16_chunking_within_tolerance(lib, oracle, genome_pair, cells, strips):
+    g, o = genome_pair
+    tab = synth.level_table()
+    reads = reads_of_lengths(g, o, tab, [1500, 2000, 2500, 3100])
+    with make_classifier(g, tab, precision=0, cells_per_thread=cells, chunk_strips=strips) as clf:
+        res = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        sf, ef, sr, er = oracle_classify(oracle, clf, reads.raw, reads.offsets)
+    np.testing.assert_allclose(res["score_fwd"], sf, rtol=FP16_RTOL)
+    np.testing.assert_allclose(res["score_rev"], sr, rtol=FP16_RTOL)
+
+
+def test_edge_cases(lib, oracle):
+    import dtwax_gb300 as d
+    tab = synth.level_table()
+    tiny = small_genome(50, 9)  # 45 columns: less than one strip
+    with make_classifier(tiny, tab, precision=1) as clf:
+        assert clf.classify(raw=np.zeros(0, np.float32), offsets=np.zeros(1, np.int64)).size == 0
+        raw = np.random.default_rng(0).normal(90, 10, 300).astype(np.float32)
+        offs = np.array([0, 0, 1, 300])  # empty read, 1-sample read, 299-sample read
+        res = clf.classify(raw=raw, offsets=offs)
+        assert res["call"][0] == -1 and res["n_samples"][0] == 0 and np.isinf(res["score"][0])
+        sf, ef, sr, er = oracle_classify(oracle, clf, raw, offs)
+        np.testing.assert_allclose(res["score_fwd"][1:], sf[1:], rtol=FP32_RTOL, atol=1e-6)
+        np.testing.assert_allclose(res["score_rev"][1:], sr[1:], rtol=FP32_RTOL, atol=1e-6)
+        with pytest.raises(d.DtwxError):
+            clf.classify(raw=raw, offsets=np.array([0, 200, 100]))  # decreasing offsets
+    # reference window semantics: adapter skip + fixed query length, short reads skipped
+    g = small_genome(8_000, 2)
+    with make_classifier(g, tab, precision=1, adapter_skip=100, query_len=500, require_full=1) as clf:
+        raw = np.random.default_rng(1).normal(90, 10, 1200).astype(np.float32)
+        offs = np.array([0, 599, 1200])  # 599 < 600 -> skipped; 601 -> window [100, 600)
+        res = clf.classify(raw=raw, offsets=offs)
+        assert res["call"][0] == -1 and res["n_samples"][1] == 500
+        sf, ef, sr, er = oracle_classify(oracle, clf, raw[599:], np.array([0, 601]), query_len=500, skip=100)
+        assert res["score_fwd"][1] == pytest.approx(sf[0], rel=FP32_RTOL)
+
+
+def test_int16_adc_scaling(lib, genome_pair):
+    """pA = (raw + offset) * range / digitisation before the z-score."""
+    g, o = genome_pair
+    tab = synth.level_table()
+    reads = reads_of_lengths(g, o, tab, [2000, 1500])
+    off, rng_, dig = np.float32(12.0), np.float32(1400.0), np.float32(8192.0)
+    adc = np.round(reads.raw / (rng_ / dig) - off).astype(np.int16)
+    pa = ((adc.astype(np.float32) + off) * (rng_ / dig)).astype(np.float32)
+    with make_classifier(g, tab, precision=1) as clf:
+        a = clf.classify_i16(raw=adc, offsets=reads.offsets, offset=[off] * 2, range_=[rng_] * 2,
+                             digitisation=[dig] * 2)
+        b = clf.classify(raw=pa, offsets=reads.offsets)
+    np.testing.assert_allclose(a["score"], b["score"], rtol=1e-6)
+    np.testing.assert_array_equal(a["end_pos"], b["end_pos"])
+
+
+def test_device_entry_points_match_host(lib, genome_pair):
+    import torch
+    import dtwax_gb300 as d
+    g, o = genome_pair
+    tab = synth.level_table()
+    reads = reads_of_lengths(g, o, tab, [2000, 1000, 3000])
+    with make_classifier(g, tab, precision=0) as clf:
+        host = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        draw = torch.tensor(reads.raw, device="cuda")
+        dout = torch.zeros(32 * reads.n, dtype=torch.uint8, device="cuda")
+        s = torch.cuda.current_stream().cuda_stream
+        clf.classify_device(draw.data_ptr(), reads.offsets, dout.data_ptr(), s)
+        torch.cuda.synchronize()
+        dev = np.frombuffer(dout.cpu().numpy().tobytes(), d.RESULT_DTYPE)
+        assert clf.last_launch_count >= 3
+    np.testing.assert_array_equal(dev["score"], host["score"])
+    np.testing.assert_array_equal(dev["end_pos"], host["end_pos"])
+
+
+def test_plain_fp32_matches_batched(lib, genome_pair):
+    g, o = genome_pair
+    tab = synth.level_table()
+    reads = reads_of_lengths(g, o, tab, [2000, 1000, 1999, 40])
+    with make_classifier(g, tab, precision=1) as clf:
+        a = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        b = clf.classify_plain_fp32(raw=reads.raw, offsets=reads.offsets)
+        assert clf.last_launch_count >= reads.n + 2
+    np.testing.assert_array_equal(a["score_fwd"], b["score_fwd"])
+    np.testing.assert_array_equal(a["end_pos"], b["end_pos"])
+
+
+def test_targets_found_at_true_position(lib):
+    """Size-independent property at a benchmark shape (C1 genome): target reads
+    end within a few k-mers of where the simulator stopped, on the right strand,
+    and score below every non-target read."""
+    w = synth.make_workload("C1", n_reads=64)
+    with make_classifier(w.genome, w.table, precision=0) as clf:
+        res = clf.classify(raw=w.reads.raw, offsets=w.reads.offsets)
+    t = w.reads.target == 1
+    true_end = w.reads.start + w.reads.kmers - 1
+    assert (res["strand"][t] == w.reads.strand[t]).all()
+    assert (np.abs(res["end_pos"][t] - true_end[t]) <= 3).mean() >= 0.95
+    assert res["score"][t].max() < res["score"][~t].min()
+
+
+def test_c1_full_parity_fp32_and_fp16(lib, oracle):
+    """All 512 reads of the C1 workload against the FP64 oracle."""
+    w = synth.make_workload("C1")
+    with make_classifier(w.genome, w.table, precision=1) as clf:
+        r32 = clf.classify(raw=w.reads.raw, offsets=w.reads.offsets)
+        ora = oracle_classify(oracle, clf, w.reads.raw, w.reads.offsets)
+    with make_classifier(w.genome, w.table, precision=0) as clf:
+        r16 = clf.classify(raw=w.reads.raw, offsets=w.reads.offsets)
+    sf, ef, sr, er = ora
+    np.testing.assert_allclose(r32["score_fwd"], sf, rtol=FP32_RTOL)
+    np.testing.assert_allclose(r32["score_rev"], sr, rtol=FP32_RTOL)
+    best = np.minimum(sf, sr)
+    np.testing.assert_allclose(r16["score"], best, rtol=FP16_RTOL)
+    score, end, strand = oracle.combine(sf, ef, sr, er)
+    assert (r32["end_pos"] == end).mean() >= 0.999
+    # classification agreement at the oracle-tuned threshold
+    from dtwax_gb300 import threshold
+    th, acc = threshold.best_threshold(best[w.reads.target == 1], best[w.reads.target == 0])
+    agree = (threshold.call(r16["score"], th) == threshold.call(best, th)).mean()
+    assert agree >= 0.999
+
+
+def test_cli_drop_in(lib, kat, tmp_path):
+    """`dtwx_main <folder> <kmer_model> <ref.fasta>` prints the reference's
+    6-column log for a folder of reads."""
+    import dtwax_gb300 as d
+    fasta, model = write_kat_files(kat, str(tmp_path))
+    folder = tmp_path / "reads"
+    folder.mkdir()
+    rng = np.random.default_rng(5)
+    raws = []
+    for i in range(4):
+        x = (rng.normal(0, 1, 4100) * 20 + 500).astype(np.int16)
+        np.save(folder / f"read_{i:02d}.npy", x)
+        raws.append(x)
+    np.save(folder / "short.npy", np.zeros(3000, np.int16))  # < 1952 + 2048: skipped
+    side = tmp_path / "side.tsv"
+    out = subprocess.run([d.CLI_PATH, str(folder), model, fasta, "--side", str(side)], capture_output=True,
+                         text=True, check=True).stdout.splitlines()
+    assert out[0].startswith("Read_ID")
+    rows = [l.split("\t") for l in out[1:]]
+    assert len(rows) == 4 and all(len(r) == 6 for r in rows)
+    assert [r[1] for r in rows] == [f"read_{i:02d}" for i in range(4)]
+    assert all(r[2] == "2048" for r in rows)
+    with d.Classifier(fasta=fasta, kmer_model=model, adapter_skip=1952, query_len=2048, require_full=1) as clf:
+        res = clf.classify([x.astype(np.float32) for x in raws])
+    np.testing.assert_allclose([float(r[4]) for r in rows], res["score_fwd"], rtol=1e-5)
+    side_rows = [l.split("\t") for l in side.read_text().splitlines()]
+    assert len(side_rows) == 5 and side_rows[-1][-1] == "skipped"
