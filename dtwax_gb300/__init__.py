@@ -99,6 +99,7 @@ _SIGNATURES = {
     "dtwx_classify_device": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P, _P]),
     "dtwx_classify_plain_fp32": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P]),
     "dtwx_last_launch_count": (ctypes.c_int32, [_P]),
+    "dtwx_last_sweep_ms": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float)]),
     "dtwx_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                                        ctypes.POINTER(ctypes.c_int32)]),
     "dtwx_peak_probe": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_float,
@@ -268,7 +269,8 @@ class Classifier:
 
     def distances(self, d_query: int, offsets: np.ndarray, d_out: int, stream: int = 0):
         """Device-pointer entry (FullDTW::distances): d_query/d_out are device
-        addresses, offsets a host int64 array; asynchronous on `stream`."""
+        addresses, offsets a host int64 array; asynchronous on `stream`
+        (a cudaStream_t value; 0 = the legacy default stream)."""
         offsets = np.ascontiguousarray(offsets, dtype=np.int64)
         _check(self._lib.dtwx_distances(self._h, ctypes.c_void_p(d_query), offsets.ctypes.data_as(_I64P),
                                         offsets.size - 1, ctypes.c_void_p(d_out), ctypes.c_void_p(stream)), self._h)
@@ -282,6 +284,12 @@ class Classifier:
     @property
     def last_launch_count(self) -> int:
         return int(self._lib.dtwx_last_launch_count(self._h))
+
+    def last_sweep_ms(self) -> float:
+        """Device time of the last sDTW sweep kernel (CUDA events on its stream)."""
+        v = ctypes.c_float()
+        _check(self._lib.dtwx_last_sweep_ms(self._h, ctypes.byref(v)), self._h)
+        return v.value
 
     def tuning(self):
         s, g, w = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()

@@ -46,6 +46,8 @@ struct BatchCtx {
   cudaStream_t stream = nullptr;
   cudaEvent_t meta_free = nullptr;  // pinned meta blob may be rewritten
   cudaEvent_t done = nullptr;
+  cudaEvent_t sweep_beg = nullptr, sweep_end = nullptr;  // bracket the last sweep launch
+  bool sweep_timed = false;
   DevBuf raw, query, meta, keys, results, seam, flags;
   HostBuf h_raw, h_meta, h_results, h_flags;
   int64_t seam_bytes = 0;
@@ -257,8 +259,11 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
     p.n_items = (int32_t)(n_tasks * p.n_chunks);
     const int ii = inst_index(precision, sh.S);
     p.use_tma = h->tmap_ok[precision][ii] ? 1 : 0;
+    CK(h, cudaEventRecord(c.sweep_beg, st));
     CK(h, launch_sdtw(precision, sh.S, sh.warps, sh.grid, p, p.use_tma ? &h->tmap[precision][ii] : nullptr,
                       st));
+    CK(h, cudaEventRecord(c.sweep_end, st));
+    c.sweep_timed = true;
     ++launches;
   }
   if (finalize) {
@@ -350,14 +355,14 @@ int wait_meta(dtwx_handle *h, BatchCtx &c) {
 int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, int is_i16,
                     const int64_t *offsets, int n_reads, const float *sc_off, const float *sc_range,
                     const float *sc_digi, dtwx_result *out_host, dtwx_result *out_dev, cudaStream_t st,
-                    int precision, bool one_launch_per_read) {
+                    bool use_given_stream, int precision, bool one_launch_per_read) {
   if (!h) return fail(nullptr, DTWX_E_ARG, "null handle");
   if (n_reads < 0 || (n_reads > 0 && !offsets)) return fail(h, DTWX_E_ARG, "bad read batch");
   for (int r = 0; r < n_reads; ++r)
     if (offsets[r + 1] < offsets[r]) return fail(h, DTWX_E_ARG, "offsets must be non-decreasing");
   CK(h, cudaSetDevice(h->device));
   BatchCtx &c = h->ctx[0];
-  if (!st) st = c.stream;
+  if (!use_given_stream) st = c.stream;
   int launches = 0;
   const Windows w = make_windows(h->cfg, offsets, n_reads);
   const size_t es = is_i16 ? 2 : 4;
@@ -554,6 +559,8 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
     if ((e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking)) != cudaSuccess) return bad(e, "stream");
     if ((e = cudaEventCreateWithFlags(&c.meta_free, cudaEventDisableTiming)) != cudaSuccess) return bad(e, "event");
     if ((e = cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming)) != cudaSuccess) return bad(e, "event");
+    if ((e = cudaEventCreate(&c.sweep_beg)) != cudaSuccess) return bad(e, "event");
+    if ((e = cudaEventCreate(&c.sweep_end)) != cudaSuccess) return bad(e, "event");
   }
   cudaStream_t st = h->ctx[0].stream;
   if ((e = h->ref16.ensure(sizeof(__half2) * h->m_pad)) != cudaSuccess) return bad(e, "alloc ref16");
@@ -668,6 +675,8 @@ int dtwx_destroy(dtwx_handle *h) {
     c.h_results.release();
     c.h_flags.release();
     if (c.meta_free) cudaEventDestroy(c.meta_free);
+    if (c.sweep_beg) cudaEventDestroy(c.sweep_beg);
+    if (c.sweep_end) cudaEventDestroy(c.sweep_end);
     if (c.done) cudaEventDestroy(c.done);
     if (c.stream) cudaStreamDestroy(c.stream);
   }
@@ -700,7 +709,7 @@ int dtwx_classify_batch(dtwx_handle *h, const float *raw, const int64_t *offsets
   if (!h) return DTWX_E_ARG;
   if (n_reads > 0 && (!raw || !out)) return fail(h, DTWX_E_ARG, "raw/out is NULL");
   return classify_common(h, raw, nullptr, 0, offsets, n_reads, nullptr, nullptr, nullptr, out, nullptr, nullptr,
-                         h->cfg.precision, false);
+                         false, h->cfg.precision, false);
 }
 
 int dtwx_classify_batch_i16(dtwx_handle *h, const int16_t *raw, const int64_t *offsets, int32_t n_reads,
@@ -709,7 +718,7 @@ int dtwx_classify_batch_i16(dtwx_handle *h, const int16_t *raw, const int64_t *o
   if (!h) return DTWX_E_ARG;
   if (n_reads > 0 && (!raw || !out)) return fail(h, DTWX_E_ARG, "raw/out is NULL");
   return classify_common(h, raw, nullptr, 1, offsets, n_reads, offset, range, digitisation, out, nullptr,
-                         nullptr, h->cfg.precision, false);
+                         nullptr, false, h->cfg.precision, false);
 }
 
 int dtwx_classify_device(dtwx_handle *h, const float *d_raw, const int64_t *offsets, int32_t n_reads,
@@ -717,7 +726,7 @@ int dtwx_classify_device(dtwx_handle *h, const float *d_raw, const int64_t *offs
   if (!h) return DTWX_E_ARG;
   if (n_reads > 0 && (!d_raw || !d_out)) return fail(h, DTWX_E_ARG, "d_raw/d_out is NULL");
   return classify_common(h, nullptr, d_raw, 0, offsets, n_reads, nullptr, nullptr, nullptr, nullptr, d_out,
-                         static_cast<cudaStream_t>(stream), h->cfg.precision, false);
+                         static_cast<cudaStream_t>(stream), true, h->cfg.precision, false);
 }
 
 int dtwx_classify_plain_fp32(dtwx_handle *h, const float *raw, const int64_t *offsets, int32_t n_reads,
@@ -725,7 +734,7 @@ int dtwx_classify_plain_fp32(dtwx_handle *h, const float *raw, const int64_t *of
   if (!h) return DTWX_E_ARG;
   if (n_reads > 0 && (!raw || !out)) return fail(h, DTWX_E_ARG, "raw/out is NULL");
   return classify_common(h, raw, nullptr, 0, offsets, n_reads, nullptr, nullptr, nullptr, out, nullptr, nullptr,
-                         DTWX_FP32, true);
+                         false, DTWX_FP32, true);
 }
 
 int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets, int32_t n_reads,
@@ -735,7 +744,7 @@ int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets,
     return fail(h, DTWX_E_ARG, "bad arguments");
   CK(h, cudaSetDevice(h->device));
   BatchCtx &c = h->ctx[0];
-  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);  // 0 = the legacy default stream
   std::vector<Task> tasks;
   int max_len = 0;
   double sum = 0;
@@ -776,6 +785,15 @@ int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets,
 }
 
 int32_t dtwx_last_launch_count(const dtwx_handle *h) { return h ? h->last_launches : -1; }
+
+int dtwx_last_sweep_ms(dtwx_handle *h, float *ms) {
+  if (!h || !ms) return DTWX_E_ARG;
+  BatchCtx &c = h->ctx[0];
+  if (!c.sweep_timed) return fail(h, DTWX_E_STATE, "no sweep launched yet");
+  CK(h, cudaEventSynchronize(c.sweep_end));
+  CK(h, cudaEventElapsedTime(ms, c.sweep_beg, c.sweep_end));
+  return DTWX_OK;
+}
 
 int dtwx_get_tuning(const dtwx_handle *h, int32_t *cells_per_thread, int32_t *chunk_strips,
                     int32_t *warps_per_cta) {

@@ -565,7 +565,8 @@ __global__ void __launch_bounds__(256) peak_probe_kernel(int iters, float *sink)
 #pragma unroll
     for (int k = S - 1; k >= 1; --k) D[k] = P::cell(R[k], qq, D[k], D[k - 1]);
     D[0] = P::cell(R[0], qq, D[0], D[S - 1]);
-    qf = -qf;
+    // a new query sample every row, as in the sweep: (r - q)^2 cannot be hoisted
+    qf = fmaf(qf, 0.999f, 0.0137f);
   }
   V acc = D[0];
 #pragma unroll

@@ -152,9 +152,10 @@ int dtwx_classify_batch_i16(dtwx_handle *h, const int16_t *raw, const int64_t *o
  * device_last_row) (src/include/DTW.hpp:287-295).  d_query holds z-scored
  * FP32 samples on the device, read r = d_query[offsets[r] .. offsets[r+1])
  * (offsets on the HOST); d_out (device, n_reads entries) receives the results.
- * Work is enqueued on `stream` (a cudaStream_t, NULL = the handle's stream)
- * and the call returns without synchronising.  Scratch (work queue, seam
- * columns, keys) is owned by the handle. */
+ * Work is enqueued on `stream` (a cudaStream_t; 0 is the legacy default
+ * stream, as for the reference's launcher) and the call returns without
+ * synchronising.  Scratch (work queue, seam columns, keys) is owned by the
+ * handle, so calls on one handle must not overlap on different streams. */
 int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets,
                    int32_t n_reads, dtwx_result *d_out, void *stream);
 
@@ -171,6 +172,12 @@ int dtwx_classify_plain_fp32(dtwx_handle *h, const float *raw, const int64_t *of
 
 /* Kernel launches issued by the most recent classify/distances call. */
 int32_t dtwx_last_launch_count(const dtwx_handle *h);
+
+/* Device time of the most recent sDTW sweep kernel launch of a classify or
+ * distances call (CUDA events recorded on its stream right before and after
+ * the launch; waits for it to finish).  The reference prints the same kind of
+ * figure with TIMERSTOP_CUDA (src/include/hpc_helpers.hpp:93-100). */
+int dtwx_last_sweep_ms(dtwx_handle *h, float *ms);
 
 /* The tuned launch shape in use for the handle's precision. */
 int dtwx_get_tuning(const dtwx_handle *h, int32_t *cells_per_thread,
