@@ -98,6 +98,7 @@ _SIGNATURES = {
     "dtwx_distances": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P, _P]),
     "dtwx_classify_device": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P, _P]),
     "dtwx_classify_plain_fp32": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P]),
+    "dtwx_distances_static": (ctypes.c_int, [_P, ctypes.c_int64, _P, _I64P, ctypes.c_int32, ctypes.c_float, _P, _P]),
     "dtwx_last_launch_count": (ctypes.c_int32, [_P]),
     "dtwx_last_sweep_ms": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float)]),
     "dtwx_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),

@@ -591,6 +591,8 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
 
 }  // namespace
 
+void dtwx::set_create_error(const char *msg) { g_create_err = msg ? msg : ""; }
+
 // =================================================================== C ABI
 
 extern "C" {

@@ -131,6 +131,9 @@ cudaError_t launch_finalize(const unsigned long long *keys, const int32_t *n_sam
 cudaError_t launch_reset(unsigned long long *keys, int n_keys, int32_t *counter,
                          cudaStream_t s);
 
+// Record the message dtwx_last_error(NULL) reports (calls made without a handle).
+void set_create_error(const char *msg);
+
 // Issue-rate probe.
 cudaError_t launch_peak_probe(int precision, int grid, int block, int iters,
                               float *sink, cudaStream_t s);

@@ -165,6 +165,28 @@ int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets,
 int dtwx_classify_device(dtwx_handle *h, const float *d_raw, const int64_t *offsets,
                          int32_t n_reads, dtwx_result *d_out, void *stream);
 
+/* FP32 sDTW of device-resident reads with no device allocation at all.
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * a process whose GPU memory is reserved by a basecaller's pool (a foreign
+ * cudaMalloc can fail or crowd the basecaller out), or a real-time loop that
+ * cannot absorb the device-wide synchronisation cudaMalloc/cudaFree may cause.
+ * No handle is needed: the caller passes the z-scored reference as FP32 pairs
+ * (fwd, rev) per k-mer column in device memory it owns -- ref_len columns,
+ * readable up to the next multiple of 512 columns -- the z-scored reads
+ * (d_query on the device, offsets on the host) and d_out (n_reads results on
+ * the device).  Scratch (task table, work counter, seam columns, result keys)
+ * is one static device array of about 9 MiB that every GPU loading the library
+ * keeps until the process exits.  Limits: at most 4096 reads per call and 2048
+ * samples per read; larger requests return DTWX_E_CAPACITY with a message in
+ * dtwx_last_error(NULL).  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the array, so calls that overlap on the GPU
+ * (different streams, or several host threads) race and must be serialised by
+ * the caller.  Asynchronous on `stream` (0 = legacy default stream). */
+int dtwx_distances_static(const void *d_ref_pairs, int64_t ref_len, const float *d_query,
+                          const int64_t *offsets, int32_t n_reads, float threshold,
+                          dtwx_result *d_out, void *stream);
+
 /* One read per launch in FP32 (no persistent queue, no graph): the plain
  * comparator the batched path is measured against.  Host buffers. */
 int dtwx_classify_plain_fp32(dtwx_handle *h, const float *raw, const int64_t *offsets,
