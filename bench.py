@@ -148,6 +148,35 @@ def cpu_baseline(workload, n_steps: int = 1, target_s: float = CPU_TARGET_S):
             "seconds": total_t, "reads_per_s": n * n_steps / total_t}
 
 
+SERVING = {
+    # Read Until: 1,600-sample chunks every 0.4 s per channel, Poisson read
+    # starts at 1/s per channel, decision after at most 3 chunks
+    "C4": dict(genome_len=5_000_000, channels=512, budget_gb=40.0),
+    # memory-admitted stress: 3,000 channels, 12 Mb genome (96 MB FP32 row per read)
+    "C5": dict(genome_len=12_000_000, channels=3000, budget_gb=100.0),
+}
+
+
+def run_serving(name: str, precision: int, device: int, duration_s: float):
+    import dtwax_gb300 as d
+    from dtwax_gb300 import readuntil, synth
+
+    spec = SERVING[name]
+    g = synth.random_genome(spec["genome_len"], synth.GENOME_SEED)
+    o = synth.random_genome(spec["genome_len"], synth.OTHER_SEED)
+    tab = synth.level_table()
+    cfg = readuntil.ServeConfig(channels=spec["channels"], duration_s=duration_s, warmup_s=2.0)
+    reads = readuntil.make_pool(g, o, tab, cfg)
+    with d.Classifier(sequence=g, level_table=tab, precision=precision, device=device) as clf:
+        accept, reject = readuntil.calibrate(clf, reads, cfg)
+        rec = readuntil.run(clf, reads, cfg, accept, reject, state_budget_bytes=spec["budget_gb"] * 1e9)
+    rec["workload"] = (f"{name}: {spec['channels']} channels, 1,600-sample chunks every 0.4 s, Poisson read "
+                       f"starts 1/s/channel, <= 3 chunks per decision, {spec['genome_len'] // 1_000_000} Mb "
+                       f"seeded genome ({2 * (spec['genome_len'] - 5)} columns), row-state budget "
+                       f"{spec['budget_gb']:.0f} GB")
+    return rec
+
+
 def run_reference(args, rank, world):
     from dtwax_gb300 import synth
     if rank != 0:
@@ -283,6 +312,8 @@ def run_ours(args, rank, world, local):
         "check": {"target_score_max": float(res["score"][t_mask].max()),
                   "other_score_min": float(res["score"][~t_mask].min())},
     }
+    if args.serving != "none" and rank == 0:
+        line["serving"] = run_serving(args.serving, precision, local, args.serving_seconds)
     if args.reads:
         line["config"]["workload"] += f" (first {n_reads} reads only)"
     if rank == 0:
@@ -305,6 +336,9 @@ def main():
     ap.add_argument("--reads", type=int, default=0,
                     help="use only the first N reads of the workload (small cases for profiling)")
     ap.add_argument("--skip-cpu", action="store_true", help="do not time the CPU baseline")
+    ap.add_argument("--serving", choices=["none", "C4", "C5"], default="C4",
+                    help="Read Until serving simulation reported beside the batch metric")
+    ap.add_argument("--serving-seconds", type=float, default=6.0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

@@ -101,11 +101,13 @@ _SIGNATURES = {
     "dtwx_distances_static": (ctypes.c_int, [_P, ctypes.c_int64, _P, _I64P, ctypes.c_int32, ctypes.c_float, _P, _P]),
     "dtwx_last_launch_count": (ctypes.c_int32, [_P]),
     "dtwx_last_sweep_ms": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float)]),
+    "dtwx_autotune": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)]),
     "dtwx_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                                        ctypes.POINTER(ctypes.c_int32)]),
     "dtwx_peak_probe": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_float,
                                        ctypes.POINTER(ctypes.c_double)]),
-    "dtwx_serve_start": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_double, ctypes.c_int32]),
+    "dtwx_serve_start": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, ctypes.c_float,
+                                        ctypes.c_float]),
     "dtwx_submit_chunk": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_uint64, _P, ctypes.c_int32, ctypes.c_int32,
                                          ctypes.c_double]),
     "dtwx_serve_step": (ctypes.c_int, [_P]),
@@ -292,15 +294,23 @@ class Classifier:
         _check(self._lib.dtwx_last_sweep_ms(self._h, ctypes.byref(v)), self._h)
         return v.value
 
+    def autotune(self, n_reads: int, read_len: int) -> float:
+        """Time the candidate launch shapes on a synthetic batch of this size;
+        returns the best sweep time in ms (the shape is kept for such batches)."""
+        v = ctypes.c_float()
+        _check(self._lib.dtwx_autotune(self._h, n_reads, read_len, ctypes.byref(v)), self._h)
+        return v.value
+
     def tuning(self):
         s, g, w = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
         _check(self._lib.dtwx_get_tuning(self._h, ctypes.byref(s), ctypes.byref(g), ctypes.byref(w)), self._h)
         return {"cells_per_thread": s.value, "chunk_strips": g.value, "warps_per_cta": w.value}
 
     # -- Read Until serving
-    def serve_start(self, max_in_flight: int = 0, state_budget_bytes: float = 0.0, chunks_per_decision: int = 3):
-        _check(self._lib.dtwx_serve_start(self._h, max_in_flight, float(state_budget_bytes), chunks_per_decision),
-               self._h)
+    def serve_start(self, max_in_flight: int = 0, state_budget_bytes: float = 0.0, chunks_per_decision: int = 3,
+                    accept_per_sample: float = 0.0, reject_per_sample: float = 0.0):
+        _check(self._lib.dtwx_serve_start(self._h, max_in_flight, float(state_budget_bytes), chunks_per_decision,
+                                          float(accept_per_sample), float(reject_per_sample)), self._h)
 
     def submit_chunk(self, channel: int, read_number: int, samples: np.ndarray, is_last: bool = False,
                      arrival_ms: float = -1.0):

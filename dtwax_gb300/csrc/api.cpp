@@ -88,7 +88,15 @@ struct dtwx_handle {
   CUtensorMap tmap[2][2]{};  // [precision][instance index]
   bool tmap_ok[2][2]{};
   Shape fixed[2];            // user-fixed parts of the shape (0 = choose)
-  BatchCtx ctx[2];
+  // autotuned shapes by (precision, log2 tasks, log2 rows): S, warps and a
+  // factor on the analytic chunk width
+  struct Tuned {
+    int S, warps;
+    double g_scale;
+  };
+  std::map<std::tuple<int, int, int>, Tuned> tuned;
+  Shape override_shape;      // set while the autotuner times a candidate
+  BatchCtx ctx[3];           // [0] offline calls, [1] and [2] the two serving batches
   std::string err;
   int32_t last_launches = 0;
   Shape last_shape[2];
@@ -103,8 +111,9 @@ struct dtwx_handle {
   std::deque<std::pair<int32_t, uint64_t>> admit_queue;
   std::vector<dtwx_decision> decisions;
   std::vector<double> latencies;
-  std::vector<ServeTask> inflight;
-  bool batch_running = false;
+  std::vector<ServeTask> inflight[2];  // tasks of the serving batch in ctx[1 + s]
+  bool running[2] = {false, false};
+  float accept_per_sample = 0.f, reject_per_sample = 0.f;
   int64_t chunks_submitted = 0, chunks_processed = 0, reads_decided = 0, reads_deferred = 0;
   int32_t batches = 0;
   double batch_reads_sum = 0;
@@ -192,17 +201,33 @@ int choose_chunk_strips(int64_t strips_per_read, int64_t n_tasks, double mean_ro
   return best_g;
 }
 
+int log2_bucket(double x) { return x < 1.0 ? 0 : (int)std::floor(std::log2(x)); }
+
+// Launch shape of a sweep: user-fixed fields win, then an autotuned entry for
+// this (precision, batch size, read length) bucket, then the defaults; the
+// chunk width comes from the analytic model (times the tuned factor).
 Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_rows) {
   Shape s;
   const Shape &f = h->fixed[precision];
-  s.S = f.S ? f.S : (precision == 0 ? 32 : 16);
-  s.warps = f.warps ? f.warps : 8;
+  const Shape &o = h->override_shape;
+  double g_scale = 1.0;
+  auto t = h->tuned.find(std::make_tuple(precision, log2_bucket((double)n_tasks), log2_bucket(mean_rows)));
+  const bool use_t = t != h->tuned.end();
+  s.S = o.S ? o.S : (f.S ? f.S : (use_t ? t->second.S : (precision == 0 ? 32 : 16)));
+  s.warps = o.warps ? o.warps : (f.warps ? f.warps : (use_t ? t->second.warps : 8));
+  if (use_t && !f.G) g_scale = t->second.g_scale;
+  if (o.S) g_scale = o.items > 0 ? o.items / 1000.0 : 1.0;  // candidate factor (per mille) while tuning
   int occ = sdtw_ctas_per_sm(precision, s.S, s.warps);
   if (occ <= 0) occ = 1;
   const int W = kWarp * s.S;
   const int64_t strips = (h->m_cols + W - 1) / W;
   const int64_t total_warps = (int64_t)h->sms * occ * s.warps;
-  s.G = f.G ? f.G : choose_chunk_strips(strips, std::max<int64_t>(n_tasks, 1), mean_rows, W, total_warps);
+  if (f.G && !o.S) {
+    s.G = f.G;
+  } else {
+    const int g0 = choose_chunk_strips(strips, std::max<int64_t>(n_tasks, 1), mean_rows, W, total_warps);
+    s.G = std::max(1, (int)std::lround(g0 * g_scale));
+  }
   if (s.G > strips) s.G = (int)strips;
   const int64_t chunks = (strips + s.G - 1) / s.G;
   const int64_t items = n_tasks * chunks;
@@ -231,7 +256,11 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
   const int64_t need = per_warp * (int64_t)sh.grid * sh.warps;
   CK(h, c.seam.ensure((size_t)need));
   CK(h, c.keys.ensure(sizeof(unsigned long long) * 2 * (size_t)std::max(n_slots, 1)));
-  CK(h, c.flags.ensure(64));
+  if (!c.flags.p) {
+    // counter and error flags start at zero; errors stay set until the host reads them
+    CK(h, c.flags.ensure(64));
+    CK(h, cudaMemsetAsync(c.flags.p, 0, 64, st));
+  }
   int32_t *counter = c.flags.as<int32_t>();
   int32_t *err = counter + 4;
   CK(h, launch_reset(c.keys.as<unsigned long long>(), 2 * n_slots, counter, st));
@@ -276,7 +305,9 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
 
 int check_device_flags(dtwx_handle *h, BatchCtx &c) {
   int32_t f[8] = {0};
+  if (!c.flags.p) return DTWX_OK;
   CK(h, cudaMemcpy(f, c.flags.p, sizeof(f), cudaMemcpyDeviceToHost));
+  if (f[4]) CK(h, cudaMemset(c.flags.as<int32_t>() + 4, 0, sizeof(int32_t)));  // reported once
   if (f[4] & kErrTmaTimeout) return fail(h, DTWX_E_TIMEOUT, "device: TMA wait gave up");
   if (f[4] & kErrBadTask) return fail(h, DTWX_E_CAPACITY, "device: task longer than the seam buffers");
   return DTWX_OK;
@@ -786,6 +817,63 @@ int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets,
   return rc;
 }
 
+int dtwx_autotune(dtwx_handle *h, int32_t n_reads, int32_t read_len, float *best_ms) {
+  if (!h || n_reads <= 0 || read_len <= 0) return DTWX_E_ARG;
+  CK(h, cudaSetDevice(h->device));
+  const int prec = h->cfg.precision;
+  // synthetic z-scored reads of the requested shape (the sweep's cost does not
+  // depend on the sample values)
+  std::vector<float> q((size_t)n_reads * read_len);
+  uint64_t x = 0x9e3779b97f4a7c15ull;
+  for (auto &v : q) {
+    x ^= x << 13, x ^= x >> 7, x ^= x << 17;
+    v = (float)((double)(x >> 11) * (1.0 / 9007199254740992.0) * 3.4641016 - 1.7320508);  // mean 0, var 1
+  }
+  DevBuf dq, dout;
+  CK(h, dq.ensure(sizeof(float) * q.size()));
+  CK(h, dout.ensure(sizeof(dtwx_result) * (size_t)n_reads));
+  CK(h, cudaMemcpy(dq.p, q.data(), sizeof(float) * q.size(), cudaMemcpyHostToDevice));
+  std::vector<int64_t> offs((size_t)n_reads + 1);
+  for (int r = 0; r <= n_reads; ++r) offs[r] = (int64_t)r * read_len;
+  BatchCtx &c = h->ctx[0];
+  cudaStream_t st = c.stream;
+  struct Cand { int S, warps, permille; };
+  std::vector<Cand> cands;
+  const int s_list[2] = {inst_S(prec, 0), inst_S(prec, 1)};
+  for (int si = 0; si < 2; ++si)
+    for (int w : {4, 8})
+      for (int pm : {500, 1000, 2000}) {
+        if (!sdtw_ctas_per_sm(prec, s_list[si], w)) continue;
+        cands.push_back({s_list[si], w, pm});
+      }
+  float best = 1e30f;
+  Cand win{0, 0, 1000};
+  int rc = DTWX_OK;
+  for (const Cand &cd : cands) {
+    h->override_shape = Shape{};
+    h->override_shape.S = cd.S;
+    h->override_shape.warps = cd.warps;
+    h->override_shape.items = cd.permille;
+    float ms = 0.f;
+    for (int rep = 0; rep < 2 && rc == DTWX_OK; ++rep) {  // first run warms this shape up
+      rc = dtwx_distances(h, dq.as<float>(), offs.data(), n_reads, dout.as<dtwx_result>(), st);
+      if (rc == DTWX_OK) rc = dtwx_last_sweep_ms(h, &ms);
+    }
+    if (rc != DTWX_OK) break;
+    if (ms < best) {
+      best = ms;
+      win = cd;
+    }
+  }
+  h->override_shape = Shape{};
+  if (rc != DTWX_OK) return rc;
+  CK(h, cudaStreamSynchronize(st));
+  h->tuned[std::make_tuple(prec, log2_bucket(n_reads), log2_bucket(read_len))] =
+      dtwx_handle::Tuned{win.S, win.warps, win.permille / 1000.0};
+  if (best_ms) *best_ms = best;
+  return DTWX_OK;
+}
+
 int32_t dtwx_last_launch_count(const dtwx_handle *h) { return h ? h->last_launches : -1; }
 
 int dtwx_last_sweep_ms(dtwx_handle *h, float *ms) {
@@ -861,13 +949,19 @@ double dtwx_now_ms(void) { return now_ms(); }
 // ----------------------------------------------------------------- serving
 
 int dtwx_serve_start(dtwx_handle *h, int32_t max_in_flight, double state_budget_bytes,
-                     int32_t chunks_per_decision) {
+                     int32_t chunks_per_decision, float accept_per_sample, float reject_per_sample) {
   if (!h) return DTWX_E_ARG;
   if (h->serving) return fail(h, DTWX_E_STATE, "serving already started");
   if (chunks_per_decision <= 0) return fail(h, DTWX_E_ARG, "chunks_per_decision must be > 0");
   CK(h, cudaSetDevice(h->device));
   const double slot_bytes = (double)h->m_pad * sizeof(float2);
   int64_t slots = max_in_flight > 0 ? max_in_flight : 0;
+  if (slots == 0 && state_budget_bytes <= 0) {
+    // neither given: the row-state pool may take half of the free device memory
+    size_t free_b = 0, total_b = 0;
+    CK(h, cudaMemGetInfo(&free_b, &total_b));
+    state_budget_bytes = std::min(0.5 * (double)free_b, 4096.0 * slot_bytes);
+  }
   if (state_budget_bytes > 0) {
     const int64_t by_budget = (int64_t)(state_budget_bytes / slot_bytes);
     slots = slots > 0 ? std::min(slots, by_budget) : by_budget;
@@ -876,6 +970,8 @@ int dtwx_serve_start(dtwx_handle *h, int32_t max_in_flight, double state_budget_
   CK(h, h->state.ensure((size_t)(slot_bytes * slots)));
   h->max_in_flight = (int32_t)slots;
   h->chunks_per_decision = chunks_per_decision;
+  h->accept_per_sample = accept_per_sample;
+  h->reject_per_sample = reject_per_sample;
   h->free_slots.clear();
   for (int64_t i = slots - 1; i >= 0; --i) h->free_slots.push_back((int)i);
   h->serving = true;
@@ -939,14 +1035,20 @@ void release_read(dtwx_handle *h, std::map<std::pair<int32_t, uint64_t>, ServeRe
   }
 }
 
-int harvest(dtwx_handle *h) {
-  BatchCtx &c = h->ctx[1];
+// Turn the results of serving batch `slot` into decisions.  After each chunk:
+// target when the score (or the score per aligned sample, if an accept rate
+// was given) is below the threshold; an early non-target when the score per
+// sample is above the reject rate; otherwise a final non-target once
+// chunks_per_decision chunks (or the read's last chunk) are aligned.
+int harvest(dtwx_handle *h, int slot) {
+  BatchCtx &c = h->ctx[1 + slot];
   CK(h, cudaEventSynchronize(c.done));
   if (int rc = check_device_flags(h, c)) return rc;
   const dtwx_result *res = c.h_results.as<dtwx_result>();
   const double t = now_ms();
-  for (size_t i = 0; i < h->inflight.size(); ++i) {
-    const ServeTask &st = h->inflight[i];
+  std::vector<ServeTask> &inflight = h->inflight[slot];
+  for (size_t i = 0; i < inflight.size(); ++i) {
+    const ServeTask &st = inflight[i];
     auto it = h->reads.find(st.key);
     if (it == h->reads.end()) continue;
     ServeRead &r = it->second;
@@ -963,9 +1065,11 @@ int harvest(dtwx_handle *h) {
     d.chunks = r.chunks_done;
     d.samples = r.samples_done;
     d.latency_ms = t - st.arrival;
-    const bool target = res[i].score < h->cfg.threshold;
+    const double per = (double)res[i].score / std::max(r.samples_done, 1);
+    const bool target = h->accept_per_sample > 0 ? per < h->accept_per_sample : res[i].score < h->cfg.threshold;
+    const bool reject = h->reject_per_sample > 0 && per > h->reject_per_sample;
     d.call = target ? 1 : 0;
-    d.decided = (target || r.chunks_done >= h->chunks_per_decision || st.last) ? 1 : 0;
+    d.decided = (target || reject || r.chunks_done >= h->chunks_per_decision || st.last) ? 1 : 0;
     h->decisions.push_back(d);
     if (d.decided) {
       h->latencies.push_back(d.latency_ms);
@@ -973,8 +1077,22 @@ int harvest(dtwx_handle *h) {
       release_read(h, it);
     }
   }
-  h->inflight.clear();
-  h->batch_running = false;
+  inflight.clear();
+  h->running[slot] = false;
+  return DTWX_OK;
+}
+
+// Harvest every serving batch that has finished; `wait` blocks for running ones.
+int harvest_done(dtwx_handle *h, bool wait) {
+  for (int s = 0; s < 2; ++s) {
+    if (!h->running[s]) continue;
+    if (!wait) {
+      const cudaError_t q = cudaEventQuery(h->ctx[1 + s].done);
+      if (q == cudaErrorNotReady) continue;
+      if (q != cudaSuccess) return fail(h, DTWX_E_CUDA, cudaGetErrorString(q));
+    }
+    if (int rc = harvest(h, s)) return rc;
+  }
   return DTWX_OK;
 }
 
@@ -984,13 +1102,14 @@ int dtwx_serve_step(dtwx_handle *h) {
   if (!h) return DTWX_E_ARG;
   if (!h->serving) return fail(h, DTWX_E_STATE, "call dtwx_serve_start first");
   CK(h, cudaSetDevice(h->device));
-  BatchCtx &c = h->ctx[1];
-  if (h->batch_running) {
-    const cudaError_t q = cudaEventQuery(c.done);
-    if (q == cudaErrorNotReady) return 0;
-    if (q != cudaSuccess) return fail(h, DTWX_E_CUDA, cudaGetErrorString(q));
-    if (int rc = harvest(h)) return rc;
-  }
+  if (int rc = harvest_done(h, false)) return rc;
+  // Continuous batching: up to two batches are in flight, each on its own
+  // stream with its own scratch; a new batch starts as soon as a slot is free,
+  // so chunks that arrive while a batch runs reach the GPU without waiting for
+  // it to end.  A read is in at most one batch at a time (its row state).
+  const int slot = !h->running[0] ? 0 : (!h->running[1] ? 1 : -1);
+  if (slot < 0) return 0;
+  BatchCtx &c = h->ctx[1 + slot];
   // decided reads whose remaining chunks are moot are dropped at decision time;
   // gather one chunk per admitted read that has one waiting
   std::vector<ServeTask> batch;
@@ -1064,8 +1183,8 @@ int dtwx_serve_step(dtwx_handle *h) {
     return rc;
   CK(h, cudaMemcpyAsync(c.h_results.p, c.results.p, sizeof(dtwx_result) * nb, cudaMemcpyDeviceToHost, st));
   CK(h, cudaEventRecord(c.done, st));
-  h->inflight = batch;
-  h->batch_running = true;
+  h->inflight[slot] = batch;
+  h->running[slot] = true;
   h->batches += 1;
   h->batch_reads_sum += nb;
   h->last_launches = launches;
@@ -1074,8 +1193,7 @@ int dtwx_serve_step(dtwx_handle *h) {
 
 int dtwx_poll_decisions(dtwx_handle *h, dtwx_decision *out, int32_t cap) {
   if (!h || (cap > 0 && !out)) return DTWX_E_ARG;
-  if (h->batch_running && cudaEventQuery(h->ctx[1].done) == cudaSuccess)
-    if (int rc = harvest(h)) return rc;
+  if (int rc = harvest_done(h, false)) return rc;
   const int n = (int)std::min<size_t>((size_t)std::max(cap, 0), h->decisions.size());
   for (int i = 0; i < n; ++i) out[i] = h->decisions[i];
   h->decisions.erase(h->decisions.begin(), h->decisions.begin() + n);
@@ -1086,11 +1204,10 @@ int dtwx_serve_drain(dtwx_handle *h) {
   if (!h) return DTWX_E_ARG;
   if (!h->serving) return fail(h, DTWX_E_STATE, "call dtwx_serve_start first");
   for (;;) {
-    if (h->batch_running)
-      if (int rc = harvest(h)) return rc;
+    if (int rc = harvest_done(h, true)) return rc;
     const int rc = dtwx_serve_step(h);
     if (rc < 0) return rc;
-    if (rc == 0 && !h->batch_running) break;
+    if (rc == 0 && !h->running[0] && !h->running[1]) break;
   }
   return DTWX_OK;
 }

@@ -1,0 +1,169 @@
+"""Read Until loop over the ctypes serving API, with a simulated sequencer.
+
+Replaces the reference's FIFO protocol (src/ReadUntil/ont_readuntil.py:29-59
+feeding src/ru_main.cu:172-326, and the fake sequencer
+src/ReadUntil/simulate_minion.py): chunks go straight into the library, each
+read's last DP row stays on the GPU between its chunks, and a decision
+(target / eject) comes back per read.
+
+`SimulatedSequencer` produces, in real time, `channels` channels; a channel
+carries one read at a time, a new read starts after an exponential gap (mean
+1 / read_rate s), and an active read delivers one chunk of `chunk` samples every
+`period_s` seconds until the library decides it (or its last chunk is sent).
+Reads come from a pool of seeded synthetic squiggles (targets from the target
+genome, others from a second genome).  Latency is measured from the scheduled
+arrival of a read's last needed chunk to its decision.
+"""
+from __future__ import annotations
+
+import heapq
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import synth
+
+
+@dataclass
+class ServeConfig:
+    channels: int = 512
+    chunk: int = 1600
+    period_s: float = 0.4
+    read_rate: float = 1.0          # read starts per second per channel
+    chunks_per_read: int = 3        # chunks available per read (and max before deciding)
+    duration_s: float = 10.0        # measured window
+    warmup_s: float = 2.0
+    target_fraction: float = 0.5
+    pool_reads: int = 1024
+    seed: int = 7
+
+
+def make_pool(genome: bytes, other: bytes, table, cfg: ServeConfig):
+    n = cfg.pool_reads
+    rng = np.random.default_rng(cfg.seed)
+    mask = (rng.random(n) < cfg.target_fraction).astype(np.int8)
+    reads = synth.simulate_reads(genome, other, table, [cfg.chunk * cfg.chunks_per_read] * n, mask,
+                                 seed=cfg.seed + 1)
+    return reads
+
+
+def calibrate(clf, reads, cfg: ServeConfig, n: int = 256):
+    """Per-sample accept / reject rates from the first chunk of n pool reads,
+    classified offline: accept below the lowest non-target rate, reject above
+    the highest target rate (so one chunk decides every read the data
+    separates, and ambiguous reads get more chunks)."""
+    n = min(n, reads.n)
+    first = [reads.read(i)[: cfg.chunk] for i in range(n)]
+    res = clf.classify(first)
+    per = res["score"] / cfg.chunk
+    t = reads.target[:n] == 1
+    if t.any() and (~t).any():
+        accept = float(min(per[~t].min(), np.quantile(per[t], 0.99)))
+        reject = float(max(per[t].max(), np.quantile(per[~t], 0.01)))
+    else:
+        accept, reject = float(np.median(per)), 0.0
+    return accept, reject
+
+
+class SimulatedSequencer:
+    def __init__(self, reads, cfg: ServeConfig):
+        self.reads = reads
+        self.cfg = cfg
+        self.rng = np.random.default_rng(cfg.seed + 2)
+        self.events = []            # (time_s, channel)
+        self.active = {}            # channel -> [read_number, pool index, next chunk k]
+        self.next_read = 1
+        self.truth = {}             # read_number -> target flag
+        t0 = 0.0
+        for ch in range(cfg.channels):
+            heapq.heappush(self.events, (t0 + self.rng.exponential(1.0 / cfg.read_rate), ch))
+
+    def due(self, now_s: float):
+        """Chunks whose arrival time has come: (arrival_s, channel, read_number, samples, is_last)."""
+        out = []
+        cfg = self.cfg
+        while self.events and self.events[0][0] <= now_s:
+            t, ch = heapq.heappop(self.events)
+            st = self.active.get(ch)
+            if st is None:  # a new read starts on this channel
+                idx = int(self.rng.integers(0, self.reads.n))
+                st = [self.next_read, idx, 0]
+                self.truth[self.next_read] = int(self.reads.target[idx])
+                self.next_read += 1
+                self.active[ch] = st
+            rn, idx, k = st
+            x = self.reads.read(idx)[k * cfg.chunk:(k + 1) * cfg.chunk]
+            last = k + 1 >= cfg.chunks_per_read
+            out.append((t, ch, rn, x, last))
+            st[2] += 1
+            if not last:
+                heapq.heappush(self.events, (t + cfg.period_s, ch))
+            else:
+                self.active.pop(ch)
+                heapq.heappush(self.events, (t + cfg.period_s + self.rng.exponential(1.0 / cfg.read_rate), ch))
+        return out
+
+    def decided(self, ch: int, rn: int, now_s: float):
+        """The library decided read rn: the sequencer stops sending its chunks
+        (ejected, or no more chunks needed) and the channel starts a new read
+        after an exponential gap."""
+        st = self.active.get(ch)
+        if st is not None and st[0] == rn:
+            self.active.pop(ch)
+            self.events = [(t, c) for (t, c) in self.events if c != ch]
+            heapq.heapify(self.events)
+            heapq.heappush(self.events, (now_s + self.rng.exponential(1.0 / self.cfg.read_rate), ch))
+
+
+def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget_bytes: float = 0.0,
+        max_in_flight: int = 0) -> dict:
+    """Real-time serving loop for warmup + duration seconds.  Returns the
+    measured-window statistics."""
+    from . import now_ms
+
+    clf.serve_start(max_in_flight=max_in_flight, state_budget_bytes=state_budget_bytes,
+                    chunks_per_decision=cfg.chunks_per_read, accept_per_sample=accept, reject_per_sample=reject)
+    seq = SimulatedSequencer(reads, cfg)
+    t_base = now_ms()
+    lat, calls, truth = [], [], []
+    decided_in_window = 0
+    chunks_in_window = 0
+    end_s = cfg.warmup_s + cfg.duration_s
+    while True:
+        now_s = (now_ms() - t_base) / 1e3
+        if now_s >= end_s:
+            break
+        for (t, ch, rn, x, last) in seq.due(now_s):
+            clf.submit_chunk(ch, rn, x, is_last=last, arrival_ms=t_base + t * 1e3)
+            if t >= cfg.warmup_s:
+                chunks_in_window += 1
+        clf.serve_step()
+        for d in clf.poll_decisions(8192):
+            if d["decided"]:
+                seq.decided(d["channel"], d["read_number"], now_s)
+                if now_s >= cfg.warmup_s:
+                    decided_in_window += 1
+                    lat.append(d["latency_ms"])
+                    calls.append(d["call"])
+                    truth.append(seq.truth.get(d["read_number"], -1))
+        time.sleep(0.0002)
+    clf.serve_drain()
+    st = clf.stats()
+    lat = np.asarray(lat)
+    calls = np.asarray(calls)
+    truth = np.asarray(truth)
+    acc = float((calls == truth).mean()) if calls.size else float("nan")
+    return {
+        "channels": cfg.channels, "chunk_samples": cfg.chunk, "duration_s": cfg.duration_s,
+        "reads_per_s": decided_in_window / cfg.duration_s,
+        "chunks_per_s": chunks_in_window / cfg.duration_s,
+        "p50_latency_ms": float(np.percentile(lat, 50)) if lat.size else None,
+        "p99_latency_ms": float(np.percentile(lat, 99)) if lat.size else None,
+        "max_latency_ms": float(lat.max()) if lat.size else None,
+        "call_accuracy": acc,
+        "mean_batch_reads": st["mean_batch_reads"], "batches": st["batches"],
+        "reads_deferred": st["reads_deferred"], "max_in_flight": st["max_in_flight"],
+        "state_bytes": st["state_bytes"],
+        "accept_per_sample": accept, "reject_per_sample": reject,
+    }

@@ -201,7 +201,15 @@ int32_t dtwx_last_launch_count(const dtwx_handle *h);
  * figure with TIMERSTOP_CUDA (src/include/hpc_helpers.hpp:93-100). */
 int dtwx_last_sweep_ms(dtwx_handle *h, float *ms);
 
-/* The tuned launch shape in use for the handle's precision. */
+/* Autotuner: time the sweep on a synthetic batch of n_reads reads of
+ * read_len samples for every compiled cells-per-thread instance, 4 and 8 warps
+ * per CTA, and half / once / twice the analytic chunk width; the fastest shape
+ * is used from then on for batches of that size (log2 buckets of read count
+ * and read length).  *best_ms gets its sweep time.  The reference fixes these
+ * at compile time (SEGMENT_SIZE, BLOCK_NUM; src/include/common.hpp:64-79). */
+int dtwx_autotune(dtwx_handle *h, int32_t n_reads, int32_t read_len, float *best_ms);
+
+/* The launch shape of the handle's most recent sweep. */
 int dtwx_get_tuning(const dtwx_handle *h, int32_t *cells_per_thread,
                     int32_t *chunk_strips, int32_t *warps_per_cta);
 
@@ -246,20 +254,26 @@ typedef struct dtwx_stats {
 } dtwx_stats;
 
 /* Prepare the handle for serving.  max_in_flight = reads holding device row
- * state at once (0: as many as state_budget_bytes allows); chunks_per_decision
+ * state at once (0: as many as state_budget_bytes allows; both 0: the pool
+ * takes half of the free device memory, at most 4096 reads); chunks_per_decision
  * = chunks after which a read is decided even if not a target (the reference
- * decides on one fixed window). */
+ * decides on one fixed window).  After each chunk a read is a target when its
+ * score per aligned sample is below accept_per_sample (or, with
+ * accept_per_sample = 0, when its score is below the config threshold), and an
+ * early non-target when its score per sample is above reject_per_sample
+ * (0 = never early). */
 int dtwx_serve_start(dtwx_handle *h, int32_t max_in_flight, double state_budget_bytes,
-                     int32_t chunks_per_decision);
+                     int32_t chunks_per_decision, float accept_per_sample,
+                     float reject_per_sample);
 
 /* Queue one chunk (FP32 pA samples) of read `read_number` on `channel`.
  * arrival_ms is the caller's clock at arrival (for latency); < 0 = now. */
 int dtwx_submit_chunk(dtwx_handle *h, int32_t channel, uint64_t read_number,
                       const float *samples, int32_t n, int32_t is_last, double arrival_ms);
 
-/* Launch one continuous-batching step if any chunk is ready (non-blocking when
- * the previous step is still running); returns the chunks launched (>= 0) or a
- * status. */
+/* Harvest finished batches and launch the next continuous batch if a chunk
+ * is ready and one of the two batch slots is free (never blocks); returns the
+ * chunks launched (>= 0) or a status. */
 int dtwx_serve_step(dtwx_handle *h);
 
 /* Collect decisions made so far (up to cap); returns the count. */

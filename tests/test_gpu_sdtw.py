@@ -275,3 +275,17 @@ def test_cli_drop_in(lib, kat, tmp_path):
     np.testing.assert_allclose([float(r[4]) for r in rows], res["score_fwd"], rtol=1e-5)
     side_rows = [l.split("\t") for l in side.read_text().splitlines()]
     assert len(side_rows) == 5 and side_rows[-1][-1] == "skipped"
+
+
+def test_autotune_picks_a_compiled_shape_and_keeps_results(lib, genome_pair):
+    g, o = genome_pair
+    tab = synth.level_table()
+    reads = reads_of_lengths(g, o, tab, [2000] * 6)
+    with make_classifier(g, tab, precision=1) as clf:
+        before = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        ms = clf.autotune(6, 2000)
+        after = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        t = clf.tuning()
+    assert ms > 0
+    assert t["cells_per_thread"] in (16, 24) and t["warps_per_cta"] in (4, 8)
+    np.testing.assert_array_equal(after["score"], before["score"])  # FP32: shape never changes the bits

@@ -1,0 +1,158 @@
+"""Read Until serving: per-read DP row state kept on the GPU between chunks.
+
+The oracle for a read served in chunks c1, c2, ... is the FP64 sDTW of
+z(c1) || z(c2) || ... where each chunk is z-scored with its own statistics
+(the serving normaliser), resumed from the previous chunk's last row; the
+decision after chunk k is the best (score, end, strand) over the last row of
+chunk k.  FP32 within 1e-5 relative with the same end column; FP16 within 1e-2.
+"""
+import numpy as np
+import pytest
+
+from gpu_util import make_classifier, small_genome
+from dtwax_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_decisions(oracle, fwd, rev, chunks):
+    """Best hit after each chunk, resumed from the saved rows."""
+    out = []
+    rf = rr = None
+    for c in chunks:
+        z = oracle.zscore(c.astype(np.float64), 1e-4).astype(np.float32).astype(np.float64)
+        sf, ef, rf = oracle.sdtw(fwd, z, init_row=rf, want_row=True)
+        sr, er, rr = oracle.sdtw(rev, z, init_row=rr, want_row=True)
+        score, end, strand = oracle.combine([sf], [ef], [sr], [er])
+        out.append((float(score[0]), int(end[0]), int(strand[0])))
+    return out
+
+
+def serve_reads(clf, reads_chunks, chunks_per_decision=3, max_in_flight=0, budget=0.0, interleave=True):
+    """Submit chunks (round-robin across reads when interleave) and drain.
+    Returns {read_number: [decision dicts in order]}."""
+    clf.serve_start(max_in_flight=max_in_flight, state_budget_bytes=budget,
+                    chunks_per_decision=chunks_per_decision)
+    rounds = max(len(c) for c in reads_chunks.values())
+    keys = list(reads_chunks)
+    if interleave:
+        for k in range(rounds):
+            for rn in keys:
+                ch = reads_chunks[rn]
+                if k < len(ch):
+                    clf.submit_chunk(rn % 512, rn, ch[k], is_last=(k == len(ch) - 1))
+            clf.serve_step()
+    else:
+        for rn in keys:
+            ch = reads_chunks[rn]
+            for k, c in enumerate(ch):
+                clf.submit_chunk(rn % 512, rn, c, is_last=(k == len(ch) - 1))
+    clf.serve_drain()
+    got = {}
+    for d in clf.poll_decisions(100000):
+        got.setdefault(d["read_number"], []).append(d)
+    return got
+
+
+def split(x, size):
+    return [x[i:i + size] for i in range(0, x.size, size)]
+
+
+@pytest.fixture(scope="module")
+def setup(built_lib, oracle):
+    g, o = small_genome(40_000, 31), small_genome(40_000, 32)
+    tab = synth.level_table()
+    reads = synth.simulate_reads(g, o, tab, [4800, 4000, 4800, 3300, 1600, 4800], [1, 0, 0, 1, 0, 0], seed=9)
+    return g, o, tab, reads
+
+
+@pytest.mark.parametrize("precision,rtol", [(1, 1e-5), (0, 1e-2)])
+def test_resume_matches_oracle(setup, oracle, precision, rtol):
+    g, o, tab, reads = setup
+    with make_classifier(g, tab, precision=precision, threshold=-1.0) as clf:  # never early: see every chunk
+        fwd, rev = clf.reference()
+        chunks = {i: split(reads.read(i), 1600) for i in range(reads.n)}
+        got = serve_reads(clf, chunks, chunks_per_decision=3)
+    for i in range(reads.n):
+        want = oracle_decisions(oracle, fwd.astype(np.float64), rev.astype(np.float64), chunks[i][:3])
+        ds = got[i]
+        assert [d["chunks"] for d in ds] == list(range(1, len(want) + 1))
+        assert ds[-1]["decided"] == 1
+        for d, (s, e, st) in zip(ds, want):
+            assert d["score"] == pytest.approx(s, rel=rtol)
+            if precision == 1:
+                assert (d["end_pos"], d["strand"]) == (e, st)
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_same_result_alone_and_in_the_mix(setup, precision):
+    """Continuous batching must not change a read's result: read 0 served alone
+    equals read 0 served while 5 other reads share its batches."""
+    g, o, tab, reads = setup
+    chunks = {i: split(reads.read(i), 1600) for i in range(reads.n)}
+    with make_classifier(g, tab, precision=precision, threshold=-1.0) as clf:
+        alone = serve_reads(clf, {0: chunks[0]})[0]
+    with make_classifier(g, tab, precision=precision, threshold=-1.0) as clf:
+        mixed = serve_reads(clf, chunks)[0]
+    assert len(alone) == len(mixed) == 3
+    for a, b in zip(alone, mixed):
+        if precision == 1:
+            assert a["score"] == b["score"] and a["end_pos"] == b["end_pos"]
+        else:
+            assert a["score"] == pytest.approx(b["score"], rel=1e-2)
+
+
+def test_admission_and_deferral(setup):
+    """Two row-state slots for six reads: four wait, all are decided, the
+    results equal unlimited admission."""
+    g, o, tab, reads = setup
+    chunks = {i: split(reads.read(i), 1600) for i in range(reads.n)}
+    with make_classifier(g, tab, precision=1, threshold=-1.0) as clf:
+        free = serve_reads(clf, chunks)
+    with make_classifier(g, tab, precision=1, threshold=-1.0) as clf:
+        tight = serve_reads(clf, chunks, max_in_flight=2)
+        st = clf.stats()
+    assert st["max_in_flight"] == 2 and st["reads_deferred"] == 4
+    assert st["reads_decided"] == reads.n and st["queue_depth"] == 0 and st["in_flight"] == 0
+    for i in range(reads.n):
+        assert [d["score"] for d in tight[i]] == [d["score"] for d in free[i]]
+    assert st["p99_latency_ms"] >= st["p50_latency_ms"] > 0
+
+
+def test_target_decided_early_and_later_chunks_ignored(setup):
+    g, o, tab, reads = setup
+    chunks = {0: split(reads.read(0), 1600)}  # read 0 is a target
+    with make_classifier(g, tab, precision=0, threshold=1e9) as clf:  # everything is a target
+        got = serve_reads(clf, chunks)
+        st = clf.stats()
+    assert len(got[0]) == 1 and got[0][0]["decided"] == 1 and got[0][0]["call"] == 1
+    assert st["chunks_processed"] == 1
+
+
+def test_state_budget_admits_by_bytes(setup):
+    import dtwax_gb300 as d
+    g, o, tab, reads = setup
+    with make_classifier(g, tab, precision=1) as clf:
+        with pytest.raises(d.DtwxError):
+            clf.serve_start(state_budget_bytes=10.0)  # not one read's row
+    with make_classifier(g, tab, precision=1) as clf:
+        # one read's row: 8 bytes per column, columns padded by less than 3072
+        clf.serve_start(state_budget_bytes=3 * 8 * (clf.ref_len + 3072.0))
+        st = clf.stats()
+        assert st["max_in_flight"] == 3 and st["state_bytes"] >= 3 * 8 * clf.ref_len
+
+
+def test_read_until_loop_real_time(built_lib):
+    """A short real-time run of the simulated sequencer through the serving API:
+    reads are decided, calls are right, latencies are recorded."""
+    from dtwax_gb300 import readuntil
+    g, o = small_genome(200_000, 41), small_genome(200_000, 42)
+    tab = synth.level_table()
+    cfg = readuntil.ServeConfig(channels=64, duration_s=2.0, warmup_s=0.5, pool_reads=128)
+    pool = readuntil.make_pool(g, o, tab, cfg)
+    with make_classifier(g, tab, precision=0) as clf:
+        accept, reject = readuntil.calibrate(clf, pool, cfg, n=128)
+        rec = readuntil.run(clf, pool, cfg, accept, reject)
+    assert rec["reads_per_s"] > 20
+    assert rec["call_accuracy"] >= 0.95
+    assert 0 < rec["p50_latency_ms"] <= rec["p99_latency_ms"] < 1000
