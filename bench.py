@@ -227,7 +227,10 @@ def run_ours(args, rank, world, local):
     cells = w.cells()
     n_reads = w.reads.n
     peak = d.peak_probe(local, precision, 400.0)
-    clf = d.Classifier(sequence=w.genome, level_table=w.table, precision=precision, device=local)
+    clf = d.Classifier(sequence=w.genome, level_table=w.table, precision=precision, device=local,
+                       cells_per_thread=args.cells, chunk_strips=args.strips, warps_per_cta=args.warps)
+    if args.autotune:
+        clf.autotune(n_reads, int(np.diff(w.reads.offsets).max()))
     stream = torch.cuda.Stream()
     d_raw = torch.tensor(w.reads.raw, device="cuda")
     d_out = torch.zeros(32 * n_reads, dtype=torch.uint8, device="cuda")
@@ -260,6 +263,7 @@ def run_ours(args, rank, world, local):
             sweep_ms.append(clf.last_sweep_ms())
     barrier()
     clock_rec = clocks.stop()
+    tuning = clf.tuning()
     total_ms = max_over_ranks(sum(step_ms))
     res = np.frombuffer(d_out.cpu().numpy().tobytes(), d.RESULT_DTYPE)
 
@@ -295,7 +299,7 @@ def run_ours(args, rank, world, local):
                    "reads_per_step": n_reads, "ref_columns_per_strand": w.ref_len,
                    "precision": args.precision, "step": "window+z-score kernel, sDTW sweep, min/argmin finalize; "
                    "raw samples resident in HBM", "l2": "flushed between timed steps (256 MB write)",
-                   "tuning": clf.tuning(), "seeds": w.meta["seeds"], "parallelism": f"replicas x{world}"},
+                   "tuning": tuning, "seeds": w.meta["seeds"], "parallelism": f"replicas x{world}"},
         "reads_per_s": reads_per_s,
         "roofline": {"bound": "alu", "achieved": achieved, "peak": peak / 1e9, "unit": "Gcell/s",
                      "frac": achieved / (peak / 1e9), "traffic": traffic,
@@ -339,6 +343,10 @@ def main():
     ap.add_argument("--serving", choices=["none", "C4", "C5"], default="C4",
                     help="Read Until serving simulation reported beside the batch metric")
     ap.add_argument("--serving-seconds", type=float, default=6.0)
+    ap.add_argument("--cells", type=int, default=0, help="cells per thread (0 = tuned)")
+    ap.add_argument("--strips", type=int, default=0, help="strips per work item (0 = tuned)")
+    ap.add_argument("--warps", type=int, default=0, help="warps per CTA (0 = tuned)")
+    ap.add_argument("--autotune", action="store_true", help="time candidate launch shapes before measuring")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

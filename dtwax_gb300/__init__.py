@@ -102,8 +102,7 @@ _SIGNATURES = {
     "dtwx_last_launch_count": (ctypes.c_int32, [_P]),
     "dtwx_last_sweep_ms": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float)]),
     "dtwx_autotune": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)]),
-    "dtwx_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
-                                       ctypes.POINTER(ctypes.c_int32)]),
+    "dtwx_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]),
     "dtwx_peak_probe": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_float,
                                        ctypes.POINTER(ctypes.c_double)]),
     "dtwx_serve_start": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, ctypes.c_float,
@@ -302,9 +301,11 @@ class Classifier:
         return v.value
 
     def tuning(self):
-        s, g, w = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
-        _check(self._lib.dtwx_get_tuning(self._h, ctypes.byref(s), ctypes.byref(g), ctypes.byref(w)), self._h)
-        return {"cells_per_thread": s.value, "chunk_strips": g.value, "warps_per_cta": w.value}
+        """Launch shape of the most recent batched sweep."""
+        v = (ctypes.c_int32 * 6)()
+        _check(self._lib.dtwx_get_tuning(self._h, v, 6), self._h)
+        keys = ("cells_per_thread", "chunk_strips", "warps_per_cta", "ctas", "work_items", "ctas_per_sm")
+        return dict(zip(keys, list(v)))
 
     # -- Read Until serving
     def serve_start(self, max_in_flight: int = 0, state_budget_bytes: float = 0.0, chunks_per_decision: int = 3,

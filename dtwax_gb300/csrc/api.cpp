@@ -85,8 +85,8 @@ struct dtwx_handle {
   int64_t m_cols = 0;  // DP columns (m, or 2m for the concatenated mode)
   int64_t m_pad = 0;
   DevBuf ref16, ref32, fwd32, rev32;
-  CUtensorMap tmap[2][2]{};  // [precision][instance index]
-  bool tmap_ok[2][2]{};
+  CUtensorMap tmap[2][3]{};  // [precision][instance index]
+  bool tmap_ok[2][3]{};
   Shape fixed[2];            // user-fixed parts of the shape (0 = choose)
   // autotuned shapes by (precision, log2 tasks, log2 rows): S, warps and a
   // factor on the analytic chunk width
@@ -137,14 +137,15 @@ int fail(dtwx_handle *h, int code, const std::string &msg) {
                   std::string(#call) + ": " + cudaGetErrorString(_e));                      \
   } while (0)
 
+// compiled sweep instances (cells per lane) by precision
+constexpr int kInstS[2][3] = {{32, 48, 0}, {16, 32, 48}};
+int inst_count(int precision) { return precision == 0 ? 2 : 3; }
 int inst_index(int precision, int S) {
-  if (precision == 0) return S == 48 ? 1 : 0;
-  return S == 24 ? 1 : 0;
+  for (int i = 0; i < inst_count(precision); ++i)
+    if (kInstS[precision][i] == S) return i;
+  return 0;
 }
-int inst_S(int precision, int idx) {
-  if (precision == 0) return idx ? 48 : 32;
-  return idx ? 24 : 16;
-}
+int inst_S(int precision, int idx) { return kInstS[precision][idx]; }
 
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -159,16 +160,18 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
-// The reference pairs viewed as rows of 128 bytes (32 x u32); one box = one
-// strip (32 lanes x S pairs), loaded with 128-byte swizzling so that each lane's
-// 16-byte reads of its own slice are free of bank conflicts.
-bool make_tmap(CUtensorMap *map, void *base, int64_t m_pad, int pair_bytes, int S) {
+// The reference viewed as rows of 128 bytes (32 x u32); one box = one strip
+// (32 lanes x S four-byte elements), loaded with 128-byte swizzling so that
+// each lane's 16-byte reads of its own slice are free of bank conflicts.
+// `elems` = 4-byte elements in the buffer (m_pad pairs for FP16, two planes
+// of m_pad floats for FP32).
+bool make_tmap(CUtensorMap *map, void *base, int64_t elems, int S) {
   auto enc = tensor_map_encoder();
   if (!enc) return false;
-  const cuuint64_t rows = (cuuint64_t)(m_pad * pair_bytes / 128);
+  const cuuint64_t rows = (cuuint64_t)(elems * 4 / 128);
   cuuint64_t dims[2] = {32, rows};
   cuuint64_t strides[1] = {128};
-  cuuint32_t box[2] = {32, (cuuint32_t)(32 * S * pair_bytes / 128)};
+  cuuint32_t box[2] = {32, (cuuint32_t)(32 * S * 4 / 128)};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, base, dims, strides, box, estr,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -213,7 +216,7 @@ Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_row
   double g_scale = 1.0;
   auto t = h->tuned.find(std::make_tuple(precision, log2_bucket((double)n_tasks), log2_bucket(mean_rows)));
   const bool use_t = t != h->tuned.end();
-  s.S = o.S ? o.S : (f.S ? f.S : (use_t ? t->second.S : (precision == 0 ? 32 : 16)));
+  s.S = o.S ? o.S : (f.S ? f.S : (use_t ? t->second.S : 32));
   s.warps = o.warps ? o.warps : (f.warps ? f.warps : (use_t ? t->second.warps : 8));
   if (use_t && !f.G) g_scale = t->second.g_scale;
   if (o.S) g_scale = o.items > 0 ? o.items / 1000.0 : 1.0;  // candidate factor (per mille) while tuning
@@ -246,7 +249,7 @@ char *align16(char *p) { return reinterpret_cast<char *>((reinterpret_cast<uintp
 int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, const float *d_query,
                   const Task *d_tasks, const int32_t *d_order, int64_t n_tasks, int max_rows,
                   double mean_rows, int n_slots, const int32_t *d_nsamp, void *d_out,
-                  float2 *state, bool finalize, int &launches) {
+                  float *state, bool finalize, int &launches) {
   Shape sh = pick_shape(h, precision, n_tasks, mean_rows);
   h->last_shape[precision] = sh;
   const int pb = sdtw_pair_bytes(precision);
@@ -254,6 +257,7 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
   if (rows_cap < 1024) rows_cap = 1024;
   const int64_t per_warp = seam_bytes_per_warp(pb, rows_cap);
   const int64_t need = per_warp * (int64_t)sh.grid * sh.warps;
+  const int strands = h->cfg.strand_mode == DTWX_STRANDS_CONCAT ? 1 : 2;
   CK(h, c.seam.ensure((size_t)need));
   CK(h, c.keys.ensure(sizeof(unsigned long long) * 2 * (size_t)std::max(n_slots, 1)));
   if (!c.flags.p) {
@@ -285,7 +289,9 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
     p.n_chunks = (int32_t)((strips + sh.G - 1) / sh.G);
     p.chunk_strips = sh.G;
     p.max_rows = rows_cap;
-    p.n_items = (int32_t)(n_tasks * p.n_chunks);
+    p.n_items = (int32_t)(n_tasks * p.n_chunks * (precision == 1 ? strands : 1));
+    p.ref_layout = 1;
+    p.strands = strands;
     const int ii = inst_index(precision, sh.S);
     p.use_tma = h->tmap_ok[precision][ii] ? 1 : 0;
     CK(h, cudaEventRecord(c.sweep_beg, st));
@@ -487,7 +493,6 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
     for (int64_t t = 0; t < n_tasks; ++t) {
       // the keys were reset once above; each read gets its own sweep launch
       const Shape sh = pick_shape(h, precision, 1, tasks[t].n);
-      h->last_shape[precision] = sh;
       int32_t *counter = c.flags.as<int32_t>();
       CK(h, cudaMemsetAsync(counter, 0, sizeof(int32_t), st));
       SdtwParams p{};
@@ -508,7 +513,9 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
       p.n_chunks = (int32_t)((strips + sh.G - 1) / sh.G);
       p.chunk_strips = sh.G;
       p.max_rows = rows_cap;
-      p.n_items = p.n_chunks;
+      p.strands = h->cfg.strand_mode == DTWX_STRANDS_CONCAT ? 1 : 2;
+      p.n_items = p.n_chunks * (precision == 1 ? p.strands : 1);
+      p.ref_layout = 1;
       const int ii = inst_index(precision, sh.S);
       p.use_tma = h->tmap_ok[precision][ii] ? 1 : 0;
       CK(h, launch_sdtw(precision, sh.S, sh.warps, sh.grid, p, p.use_tma ? &h->tmap[precision][ii] : nullptr,
@@ -595,7 +602,7 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
   }
   cudaStream_t st = h->ctx[0].stream;
   if ((e = h->ref16.ensure(sizeof(__half2) * h->m_pad)) != cudaSuccess) return bad(e, "alloc ref16");
-  if ((e = h->ref32.ensure(sizeof(float2) * h->m_pad)) != cudaSuccess) return bad(e, "alloc ref32");
+  if ((e = h->ref32.ensure(2 * sizeof(float) * h->m_pad)) != cudaSuccess) return bad(e, "alloc ref32");
   if ((e = h->fwd32.ensure(sizeof(float) * m)) != cudaSuccess) return bad(e, "alloc fwd32");
   if ((e = h->rev32.ensure(sizeof(float) * m)) != cudaSuccess) return bad(e, "alloc rev32");
   DevBuf d_seq, d_table, d_work;
@@ -606,16 +613,16 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
   cudaMemcpyAsync(d_table.p, table.data(), sizeof(double) * kTableSize, cudaMemcpyHostToDevice, st);
   e = launch_build_reference(d_seq.as<char>(), L, d_table.as<double>(), m, h->m_pad,
                              cfg.strand_mode == DTWX_STRANDS_CONCAT, d_work.as<double>(), h->ref16.as<__half2>(),
-                             h->ref32.as<float2>(), h->fwd32.as<float>(), h->rev32.as<float>(), st);
+                             h->ref32.as<float>(), h->fwd32.as<float>(), h->rev32.as<float>(), st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   d_seq.release();
   d_table.release();
   d_work.release();
   if (e != cudaSuccess) return bad(e, "reference build");
   for (int p = 0; p < 2; ++p)
-    for (int i = 0; i < 2; ++i)
-      h->tmap_ok[p][i] = make_tmap(&h->tmap[p][i], p == 0 ? h->ref16.p : h->ref32.p, h->m_pad,
-                                   sdtw_pair_bytes(p), inst_S(p, i));
+    for (int i = 0; i < inst_count(p); ++i)
+      h->tmap_ok[p][i] = make_tmap(&h->tmap[p][i], p == 0 ? h->ref16.p : h->ref32.p,
+                                   p == 0 ? h->m_pad : 2 * h->m_pad, inst_S(p, i));
   *out = h;
   return DTWX_OK;
 }
@@ -839,12 +846,11 @@ int dtwx_autotune(dtwx_handle *h, int32_t n_reads, int32_t read_len, float *best
   cudaStream_t st = c.stream;
   struct Cand { int S, warps, permille; };
   std::vector<Cand> cands;
-  const int s_list[2] = {inst_S(prec, 0), inst_S(prec, 1)};
-  for (int si = 0; si < 2; ++si)
+  for (int si = 0; si < inst_count(prec); ++si)
     for (int w : {4, 8})
       for (int pm : {500, 1000, 2000}) {
-        if (!sdtw_ctas_per_sm(prec, s_list[si], w)) continue;
-        cands.push_back({s_list[si], w, pm});
+        if (!sdtw_ctas_per_sm(prec, inst_S(prec, si), w)) continue;
+        cands.push_back({inst_S(prec, si), w, pm});
       }
   float best = 1e30f;
   Cand win{0, 0, 1000};
@@ -885,13 +891,11 @@ int dtwx_last_sweep_ms(dtwx_handle *h, float *ms) {
   return DTWX_OK;
 }
 
-int dtwx_get_tuning(const dtwx_handle *h, int32_t *cells_per_thread, int32_t *chunk_strips,
-                    int32_t *warps_per_cta) {
-  if (!h) return DTWX_E_ARG;
+int dtwx_get_tuning(const dtwx_handle *h, int32_t *out, int32_t n) {
+  if (!h || !out || n < 0) return DTWX_E_ARG;
   const Shape &s = h->last_shape[h->cfg.precision];
-  if (cells_per_thread) *cells_per_thread = s.S;
-  if (chunk_strips) *chunk_strips = s.G;
-  if (warps_per_cta) *warps_per_cta = s.warps;
+  const int32_t v[6] = {s.S, s.G, s.warps, s.grid, s.items, s.S ? sdtw_ctas_per_sm(h->cfg.precision, s.S, s.warps) : 0};
+  for (int i = 0; i < n && i < 6; ++i) out[i] = v[i];
   return DTWX_OK;
 }
 
@@ -934,7 +938,7 @@ int dtwx_peak_probe(int32_t device, int32_t precision, float ms_target, double *
     cudaEventRecord(b, s);
     if (cudaEventSynchronize(b) != cudaSuccess) rc = DTWX_E_CUDA;
     cudaEventElapsedTime(&ms, a, b);
-    const double cells = (double)grid * block * (double)iters * 32.0 * 2.0;
+    const double cells = (double)grid * block * (double)iters * 32.0 * (precision == 0 ? 2.0 : 1.0);
     *cells_per_s = cells / (ms * 1e-3);
   }
   cudaEventDestroy(a);
@@ -954,7 +958,7 @@ int dtwx_serve_start(dtwx_handle *h, int32_t max_in_flight, double state_budget_
   if (h->serving) return fail(h, DTWX_E_STATE, "serving already started");
   if (chunks_per_decision <= 0) return fail(h, DTWX_E_ARG, "chunks_per_decision must be > 0");
   CK(h, cudaSetDevice(h->device));
-  const double slot_bytes = (double)h->m_pad * sizeof(float2);
+  const double slot_bytes = 2.0 * (double)h->m_pad * sizeof(float);  // fwd and rev planes
   int64_t slots = max_in_flight > 0 ? max_in_flight : 0;
   if (slots == 0 && state_budget_bytes <= 0) {
     // neither given: the row-state pool may take half of the free device memory
@@ -1152,7 +1156,7 @@ int dtwx_serve_step(dtwx_handle *h) {
     t.q_off = off;
     t.n = batch[i].n;
     t.flags = kTaskSaveState | (r.chunks_done > 0 ? kTaskResume : 0);
-    t.state_off = (int64_t)r.slot * h->m_pad;
+    t.state_off = (int64_t)r.slot * 2 * h->m_pad;
     t.out_slot = i;
     nsamp[i] = batch[i].n;
     src_off[i] = off;
@@ -1178,7 +1182,7 @@ int dtwx_serve_step(dtwx_handle *h) {
   double mean = (double)total / nb;
   if (int rc = enqueue_sweep(h, c, h->cfg.precision, st, c.query.as<float>(), reinterpret_cast<const Task *>(dm + L.tasks),
                              reinterpret_cast<const int32_t *>(dm + L.order), nb, max_len, mean, nb,
-                             reinterpret_cast<const int32_t *>(dm + L.nsamp), c.results.p, h->state.as<float2>(), true,
+                             reinterpret_cast<const int32_t *>(dm + L.nsamp), c.results.p, h->state.as<float>(), true,
                              launches))
     return rc;
   CK(h, cudaMemcpyAsync(c.h_results.p, c.results.p, sizeof(dtwx_result) * nb, cudaMemcpyDeviceToHost, st));

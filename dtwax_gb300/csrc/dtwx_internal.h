@@ -42,11 +42,12 @@ struct SdtwParams {
   const Task *tasks;           // n_tasks
   const int32_t *order;        // processing order of tasks (longest first); NULL = identity
   unsigned long long *keys;    // 2 per out slot: (orderable score << 32) | end column
-  float2 *state;               // row-state pool (absolute FP32 values), NULL if unused
+  float *state;                // row-state pool (absolute FP32 values, per read a fwd and a rev
+                               // plane of m_pad floats), NULL if unused
   char *seam;                  // per-warp scratch (seam columns + epoch offsets)
   int32_t *counter;            // work-queue ticket counter (zeroed before launch)
   int32_t *err;                // device error flags
-  const void *ref_plain;       // ref pairs in global memory (used when TMA is off)
+  const void *ref_plain;       // reference in global memory (used when TMA is off)
   int64_t m;                   // valid columns per strand
   int64_t m_pad;               // padded columns (multiple of the strip width)
   int64_t seam_stride;         // bytes of scratch per warp
@@ -54,19 +55,22 @@ struct SdtwParams {
   int32_t n_chunks;            // chunks per task
   int32_t chunk_strips;        // strips per chunk
   int32_t max_rows;            // capacity of the seam buffers (rows)
-  int32_t n_items;             // n_tasks * n_chunks
+  int32_t n_items;             // informational: the kernel derives the queue length itself
   int32_t use_tma;
+  int32_t ref_layout;          // FP32: 0 = interleaved (fwd, rev) float pairs, 1 = planar (rev plane at m_pad)
+  int32_t strands;             // FP32 strands per task: 2 (paired), 1 (concatenated sequence); 0 = 2
 };
 
-// Per-warp scratch layout, in bytes, for a pair type of `pair_bytes` bytes.
+// Per-warp scratch layout, in bytes, for cells of `pair_bytes` bytes.
 // Each half (one per strip parity) holds the seam column, (max_rows + 1)
-// pairs, then from a 16-byte aligned position the FP32 offsets of the
-// epochs, (max_rows / kRescaleRows + 2) float2.
+// cells plus 32 of slack (whole-warp stores past the last row land there),
+// then from a 16-byte aligned position the FP32 offsets of the epochs,
+// (max_rows / kRescaleRows + 2) float2 plus 32 of slack.
 inline __host__ __device__ int64_t seam_offsets_pos(int pair_bytes, int max_rows) {
-  return ((int64_t)(max_rows + 1) * pair_bytes + 15) & ~(int64_t)15;
+  return ((int64_t)(max_rows + 1 + 32) * pair_bytes + 15) & ~(int64_t)15;
 }
 inline __host__ __device__ int64_t seam_bytes_per_warp(int pair_bytes, int max_rows) {
-  const int64_t epochs = (int64_t)(max_rows / kRescaleRows + 2) * 8;
+  const int64_t epochs = (int64_t)(max_rows / kRescaleRows + 2 + 32) * 8;
   int64_t per = seam_offsets_pos(pair_bytes, max_rows) + epochs;
   per = (per + 255) & ~(int64_t)255;
   return 2 * per;  // ping-pong between consecutive strips
@@ -107,10 +111,11 @@ int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta);
 bool sdtw_instance_exists(int precision, int cells_per_thread);
 int sdtw_pair_bytes(int precision);
 
-// Reference builder: genome bytes -> z-scored (fwd, rev) pairs in FP16 and FP32.
+// Reference builder: genome bytes -> z-scored levels as FP16 (fwd, rev) pairs
+// and as FP32 planes (fwd plane, then rev plane at m_pad).
 cudaError_t launch_build_reference(const char *d_seq, int64_t L, const double *d_table,
                                    int64_t m, int64_t m_pad, int concat, double *d_work,
-                                   __half2 *d_ref16, float2 *d_ref32, float *d_fwd32,
+                                   __half2 *d_ref16, float *d_ref32, float *d_fwd32,
                                    float *d_rev32, cudaStream_t s);
 size_t build_reference_work_bytes(int64_t m);
 

@@ -143,10 +143,12 @@ __global__ void reduce_sd_kernel(const double *partial, int nblk, double *stats)
   }
 }
 
-// Writes the z-scored pairs.  PAIRED: pair j = (fwd[j], rev[j]), j < m.
-// CONCAT: one sequence fwd||rev of 2m columns, stored twice (.x and .y).
+// Writes the z-scored levels: FP16 pairs (fwd[j], rev[j]) and FP32 planes.
+// PAIRED: column j < m holds k-mer j of each strand.  CONCAT: one sequence
+// fwd||rev of 2m columns, stored in both strand slots (the FP32 sweep then
+// aligns only plane 0).
 __global__ void zscore_pairs_kernel(const double *lev, int64_t m, int64_t m_pad, int concat,
-                                    const double *stats, __half2 *ref16, float2 *ref32,
+                                    const double *stats, __half2 *ref16, float *ref32,
                                     float *fwd32, float *rev32) {
   const double mf = stats[0], mr = stats[2];
   const double sf = stats[4] > 0 ? stats[4] : 1.0, sr = stats[5] > 0 ? stats[5] : 1.0;
@@ -168,7 +170,8 @@ __global__ void zscore_pairs_kernel(const double *lev, int64_t m, int64_t m_pad,
       b = a;
       if (rv) rev32[j - m] = a; else fwd32[j] = a;
     }
-    ref32[j] = make_float2(a, b);
+    ref32[j] = a;          // fwd plane
+    ref32[m_pad + j] = b;  // rev plane
     ref16[j] = __floats2half2_rn(a, b);
   }
 }
@@ -180,7 +183,7 @@ size_t build_reference_work_bytes(int64_t m) {
 
 cudaError_t launch_build_reference(const char *d_seq, int64_t L, const double *d_table, int64_t m,
                                    int64_t m_pad, int concat, double *d_work, __half2 *d_ref16,
-                                   float2 *d_ref32, float *d_fwd32, float *d_rev32,
+                                   float *d_ref32, float *d_fwd32, float *d_rev32,
                                    cudaStream_t s) {
   const int nblk = 1024;
   double *lev = d_work;

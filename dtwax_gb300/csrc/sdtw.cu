@@ -35,15 +35,19 @@ namespace dtwx {
 #define FULL_MASK 0xffffffffu
 
 // ---------------------------------------------------------------- precision policies
+// Both policies keep one 32-bit register per cell so that selects, shuffles
+// and seam stores are single instructions.  FP16 packs the two strands of a
+// column into one __half2 (fwd in .x, rev in .y) and a work item covers both;
+// FP32 keeps one strand per cell and a work item covers one strand.
 
 template <int PREC> struct Pol;
 
 template <> struct Pol<0> {  // FP16 pairs
   using V = __half2;
-  static constexpr int PB = 4;
+  static constexpr int EB = 4;       // bytes per cell / reference element
+  static constexpr int STRANDS = 1;  // work items per (task, chunk)
   __device__ __forceinline__ static V inf() { return __half2half2(__ushort_as_half((unsigned short)0x7c00u)); }
   __device__ __forceinline__ static V zero() { return __half2half2(__ushort_as_half((unsigned short)0)); }
-  __device__ __forceinline__ static V qv(float q) { return __float2half2_rn(q); }
   __device__ __forceinline__ static V cell(V r, V q, V a, V b) {
     const V d = __hsub2(r, q);
     return __hfma2(d, d, __hmin2(a, b));
@@ -52,42 +56,37 @@ template <> struct Pol<0> {  // FP16 pairs
   __device__ __forceinline__ static V shfl(V v, int src) { return __shfl_sync(FULL_MASK, v, src); }
   __device__ __forceinline__ static V shfl_up(V v) { return __shfl_up_sync(FULL_MASK, v, 1); }
   __device__ __forceinline__ static V shfl_xor(V v, int m) { return __shfl_xor_sync(FULL_MASK, v, m); }
-  __device__ __forceinline__ static float2 to_f2(V v) { return __half22float2(v); }
-  __device__ __forceinline__ static V from_f2(float2 f) { return __float22half2_rn(f); }
+  __device__ __forceinline__ static V sel(bool p, V a, V b) { return p ? a : b; }
+  __device__ __forceinline__ static V from_bits(uint32_t u) {
+    V v;
+    memcpy(&v, &u, 4);
+    return v;
+  }
   // query window: one half2 (q, q) per lane, broadcast by one shuffle per row
   using QW = __half2;
   __device__ __forceinline__ static QW qw(float q) { return __float2half2_rn(q); }
   __device__ __forceinline__ static V qbcast(QW w, int il) { return __shfl_sync(FULL_MASK, w, il); }
 };
 
-template <> struct Pol<1> {  // FP32 pairs
-  using V = float2;
-  static constexpr int PB = 8;
-  __device__ __forceinline__ static V inf() { return make_float2(__int_as_float(0x7f800000), __int_as_float(0x7f800000)); }
-  __device__ __forceinline__ static V zero() { return make_float2(0.f, 0.f); }
-  __device__ __forceinline__ static V qv(float q) { return make_float2(q, q); }
+template <> struct Pol<1> {  // FP32, one strand
+  using V = float;
+  static constexpr int EB = 4;
+  static constexpr int STRANDS = 2;
+  __device__ __forceinline__ static V inf() { return __int_as_float(0x7f800000); }
+  __device__ __forceinline__ static V zero() { return 0.f; }
   __device__ __forceinline__ static V cell(V r, V q, V a, V b) {
-    const float dx = r.x - q.x, dy = r.y - q.y;
-    return make_float2(fmaf(dx, dx, fminf(a.x, b.x)), fmaf(dy, dy, fminf(a.y, b.y)));
+    const float d = r - q;
+    return fmaf(d, d, fminf(a, b));
   }
-  __device__ __forceinline__ static V vmin(V a, V b) { return make_float2(fminf(a.x, b.x), fminf(a.y, b.y)); }
-  __device__ __forceinline__ static V shfl(V v, int src) {
-    return make_float2(__shfl_sync(FULL_MASK, v.x, src), __shfl_sync(FULL_MASK, v.y, src));
-  }
-  __device__ __forceinline__ static V shfl_up(V v) {
-    return make_float2(__shfl_up_sync(FULL_MASK, v.x, 1), __shfl_up_sync(FULL_MASK, v.y, 1));
-  }
-  __device__ __forceinline__ static V shfl_xor(V v, int m) {
-    return make_float2(__shfl_xor_sync(FULL_MASK, v.x, m), __shfl_xor_sync(FULL_MASK, v.y, m));
-  }
-  __device__ __forceinline__ static float2 to_f2(V v) { return v; }
-  __device__ __forceinline__ static V from_f2(float2 f) { return f; }
+  __device__ __forceinline__ static V vmin(V a, V b) { return fminf(a, b); }
+  __device__ __forceinline__ static V shfl(V v, int src) { return __shfl_sync(FULL_MASK, v, src); }
+  __device__ __forceinline__ static V shfl_up(V v) { return __shfl_up_sync(FULL_MASK, v, 1); }
+  __device__ __forceinline__ static V shfl_xor(V v, int m) { return __shfl_xor_sync(FULL_MASK, v, m); }
+  __device__ __forceinline__ static V sel(bool p, V a, V b) { return p ? a : b; }
+  __device__ __forceinline__ static V from_bits(uint32_t u) { return __uint_as_float(u); }
   using QW = float;
   __device__ __forceinline__ static QW qw(float q) { return q; }
-  __device__ __forceinline__ static V qbcast(QW w, int il) {
-    const float v = __shfl_sync(FULL_MASK, w, il);
-    return make_float2(v, v);
-  }
+  __device__ __forceinline__ static V qbcast(QW w, int il) { return __shfl_sync(FULL_MASK, w, il); }
 };
 
 // ---------------------------------------------------------------- TMA / mbarrier helpers
@@ -140,6 +139,47 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
       : "memory");
 }
 
+// Lane-0 actions as predicated PTX: every lane executes the same instruction
+// stream (the action is masked by a predicate), so the compiler never sees a
+// lane-dependent branch it could use to duplicate the whole strip loop into a
+// lane-0 copy and a lanes-1..31 copy.
+__device__ __forceinline__ void mbar_init_if(uint64_t *bar, uint32_t count, uint32_t pred) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t@p mbarrier.init.shared::cta.b64 [%0], %1;\n\t}" ::"r"(
+          smem_u32(bar)),
+      "r"(count), "r"(pred)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_issue_if(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1,
+                                             uint32_t bytes, uint32_t pred) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %5, 0;\n\t"
+      "@p mbarrier.arrive.expect_tx.shared::cta.b64 _, [%4], %6;\n\t"
+      "@p cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];\n\t}" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar)), "r"(pred), "r"(bytes)
+      : "memory");
+}
+
+// Work-queue ticket taken by lane 0 only, broadcast by the caller.
+__device__ __forceinline__ int ticket_if(int32_t *counter, uint32_t pred) {
+  int v;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\tmov.u32 %0, 0;\n\t"
+      "@p atom.global.add.u32 %0, [%1], 1;\n\t}"
+      : "=r"(v)
+      : "l"(counter), "r"(pred)
+      : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void red_min_if(unsigned long long *addr, unsigned long long v, uint32_t pred) {
+  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t@p red.global.min.u64 [%0], %1;\n\t}" ::"l"(addr),
+               "l"(v), "r"(pred)
+               : "memory");
+}
+
 // Byte offset of logical byte b of a tile written by TMA with 128-byte
 // swizzling: the 16-byte chunk index inside each 128-byte row is XOR-ed with
 // the row index modulo 8.
@@ -150,58 +190,79 @@ __device__ __forceinline__ uint32_t swz128(uint32_t b) {
 }
 
 // ---------------------------------------------------------------- ref strip -> registers
+// Lane l's slice of a strip: S consecutive 4-byte elements at byte (l*S)*4.
 
 template <int S, int PREC>
 __device__ __forceinline__ void regs_from_smem(const unsigned char *tile, int lane,
                                                typename Pol<PREC>::V (&R)[S]) {
-  using V = typename Pol<PREC>::V;
-  constexpr int PB = Pol<PREC>::PB;
-  constexpr int PER16 = 16 / PB;  // pairs per 16-byte load
-  static_assert((S * PB) % 16 == 0, "lane slice must be 16-byte aligned");
+  static_assert((S * 4) % 16 == 0, "lane slice must be 16-byte aligned");
 #pragma unroll
-  for (int k = 0; k < S; k += PER16) {
-    const uint32_t b = (uint32_t)((lane * S + k) * PB);
+  for (int k = 0; k < S; k += 4) {
+    const uint32_t b = (uint32_t)((lane * S + k) * 4);
     const uint4 v = *reinterpret_cast<const uint4 *>(tile + swz128(b));
-    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-    for (int u = 0; u < PER16; ++u) {
-      V r;
-      memcpy(&r, &w[u * (PB / 4)], PB);
-      R[k + u] = r;
-    }
+    R[k] = Pol<PREC>::from_bits(v.x);
+    R[k + 1] = Pol<PREC>::from_bits(v.y);
+    R[k + 2] = Pol<PREC>::from_bits(v.z);
+    R[k + 3] = Pol<PREC>::from_bits(v.w);
   }
 }
 
+// Contiguous elements from global memory (FP16 pairs, or one FP32 strand plane).
 template <int S, int PREC>
-__device__ __forceinline__ void regs_from_global(const void *ref, int64_t x, int lane,
+__device__ __forceinline__ void regs_from_global(const void *base_elem, int lane,
                                                  typename Pol<PREC>::V (&R)[S]) {
-  using V = typename Pol<PREC>::V;
-  constexpr int PB = Pol<PREC>::PB;
-  constexpr int PER16 = 16 / PB;
-  const unsigned char *base = reinterpret_cast<const unsigned char *>(ref) + (x + (int64_t)lane * S) * PB;
+  const uint4 *g = reinterpret_cast<const uint4 *>(reinterpret_cast<const uint32_t *>(base_elem) + lane * S);
 #pragma unroll
-  for (int k = 0; k < S; k += PER16) {
-    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(base + k * PB));
-    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-    for (int u = 0; u < PER16; ++u) {
-      V r;
-      memcpy(&r, &w[u * (PB / 4)], PB);
-      R[k + u] = r;
-    }
+  for (int k = 0; k < S; k += 4) {
+    const uint4 v = __ldg(g + k / 4);
+    R[k] = Pol<PREC>::from_bits(v.x);
+    R[k + 1] = Pol<PREC>::from_bits(v.y);
+    R[k + 2] = Pol<PREC>::from_bits(v.z);
+    R[k + 3] = Pol<PREC>::from_bits(v.w);
   }
+}
+
+// FP32 strand `strand` out of interleaved (fwd, rev) float pairs.
+template <int S>
+__device__ __forceinline__ void regs_from_pairs(const float2 *pairs, int64_t x, int lane, int strand, float (&R)[S]) {
+  const float4 *g = reinterpret_cast<const float4 *>(pairs + x + (int64_t)lane * S);
+#pragma unroll
+  for (int k = 0; k < S; k += 2) {
+    const float4 v = __ldg(g + k / 2);
+    R[k] = strand ? v.y : v.x;
+    R[k + 1] = strand ? v.w : v.z;
+  }
+}
+
+// Bit image of a cell and back (both policies use 32-bit cells).
+template <int PREC>
+__device__ __forceinline__ uint32_t cell_bits(typename Pol<PREC>::V v) {
+  uint32_t u;
+  memcpy(&u, &v, 4);
+  return u;
+}
+
+// All-ones on lane 0, zero elsewhere, from an opaque move: the optimiser cannot
+// see which lanes hold which value, so it cannot split the row loop into a
+// lane-0 copy and a lanes-1..31 copy (which halves the active lanes of every
+// cell instruction).
+__device__ __forceinline__ uint32_t lane0_mask(int lane) {
+  uint32_t m = lane == 0 ? 0xffffffffu : 0u;
+  asm volatile("mov.b32 %0, %0;" : "+r"(m));
+  return m;
 }
 
 // One DP row of this lane's S columns.  The previous row is in D; columns are
 // updated from right to left so D[k-1] still holds the previous row when
 // column k reads it.  The diagonal predecessor of column 0 comes from lane-1
-// (shuffle) or, on lane 0, from the seam column of the strip to the left.
+// (shuffle) or, on lane 0, from the seam column of the strip to the left,
+// merged in with the lane-0 bit mask.
 template <int S, int PREC>
 __device__ __forceinline__ void sweep_row(typename Pol<PREC>::V (&D)[S], const typename Pol<PREC>::V (&R)[S],
-                                          typename Pol<PREC>::V qq, typename Pol<PREC>::V seam, int lane) {
+                                          typename Pol<PREC>::V qq, typename Pol<PREC>::V seam, uint32_t m0) {
   using P = Pol<PREC>;
   const typename P::V up = P::shfl_up(D[S - 1]);
-  const typename P::V left = lane == 0 ? seam : up;
+  const typename P::V left = P::from_bits((cell_bits<PREC>(up) & ~m0) | (cell_bits<PREC>(seam) & m0));
 #pragma unroll
   for (int k = S - 1; k >= 1; --k) D[k] = P::cell(R[k], qq, D[k], D[k - 1]);
   D[0] = P::cell(R[0], qq, D[0], left);
@@ -226,22 +287,22 @@ __device__ __forceinline__ unsigned long long make_key(float v, int64_t j) {
 
 // ---------------------------------------------------------------- the persistent kernel
 
-// Register cap per instance: the S cells and S reference pairs of a lane plus
-// about 40 registers of bookkeeping, rounded to 128 or 168 (16 or 12 warps/SM).
+// Register cap per instance: the S cells and S reference elements of a lane
+// plus about 40 registers of bookkeeping, rounded to 128 or 168 (16 or 12 warps/SM).
 template <int S, int PREC>
-constexpr int sdtw_reg_cap() { return (S * Pol<PREC>::PB / 4) * 2 + 40 <= 128 ? 128 : 168; }
+constexpr int sdtw_reg_cap() { return 2 * S + 40 <= 128 ? 128 : 168; }
 
 template <int S, int PREC>
 __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_constant__ CUtensorMap tmap,
-                                                   const SdtwParams p) {
+                                                                    const SdtwParams p) {
   using P = Pol<PREC>;
   using V = typename P::V;
   constexpr int W = kWarp * S;                // columns per strip
-  constexpr int PB = P::PB;
-  constexpr int STRIP_BYTES = W * PB;
+  constexpr int EB = P::EB;
+  constexpr int STRIP_BYTES = W * EB;
   constexpr int K = kRescaleRows;
   static_assert(STRIP_BYTES % 1024 == 0, "strip tile must keep 1024-byte alignment");
-  static_assert(S % 2 == 0, "row state is moved as float4 pairs of columns");
+  static_assert(S % 4 == 0, "row state and reference move in 16-byte groups");
 
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
@@ -249,12 +310,14 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
+  const uint32_t m0 = lane0_mask(lane);
   unsigned char *const slot0 = smem + (2 * warp) * STRIP_BYTES;  // slot s at slot0 + s*STRIP_BYTES
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * nwarps * STRIP_BYTES) + 2 * warp;
 
-  if (p.use_tma && lane == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
+  const uint32_t is0 = m0 & 1u;  // 1 on lane 0 (opaque to the optimiser)
+  if (p.use_tma) {
+    mbar_init_if(&bars[0], 1, is0);
+    mbar_init_if(&bars[1], 1, is0);
     fence_mbar_init();
   }
   __syncwarp();
@@ -263,21 +326,25 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
   const int64_t gwarp = (int64_t)blockIdx.x * nwarps + warp;
   char *seam_base = p.seam + gwarp * p.seam_stride;
   const int64_t seam_half = p.seam_stride / 2;
-  const int64_t off_pos = seam_offsets_pos(PB, p.max_rows);
+  const int64_t off_pos = seam_offsets_pos(EB, p.max_rows);
   const int64_t C = (int64_t)p.chunk_strips * W;
+  // FP32 splits each (task, chunk) into one work item per strand
+  const int nstr = PREC == 1 ? (p.strands > 0 ? p.strands : 2) : 1;
+  const int per_task = p.n_chunks * nstr;
+  const int64_t n_items = (int64_t)p.n_tasks * per_task;
 
   for (;;) {
-    int item = 0;
-    if (lane == 0) item = atomicAdd(p.counter, 1);
-    item = __shfl_sync(FULL_MASK, item, 0);
-    if (item >= p.n_items) break;
-    const int tr = item / p.n_chunks;
-    const int chunk = item - tr * p.n_chunks;
+    const int item = __shfl_sync(FULL_MASK, ticket_if(p.counter, is0), 0);
+    if (item >= n_items) break;
+    const int tr = item / per_task;
+    const int rem = item - tr * per_task;
+    const int strand = PREC == 1 ? rem / p.n_chunks : 0;
+    const int chunk = rem - strand * p.n_chunks;
     const int ti = p.order ? p.order[tr] : tr;
     const Task t = p.tasks[ti];
     const int n = t.n;
     if (n <= 0 || n > p.max_rows) {
-      if (n > p.max_rows && lane == 0) atomicOr(p.err, kErrBadTask);
+      if (n > p.max_rows) atomicOr(p.err, kErrBadTask);  // every lane: same bit
       continue;
     }
     const int64_t a = (int64_t)chunk * C;
@@ -291,14 +358,17 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
     const float *q = p.query + t.q_off;
     const bool resume = (t.flags & kTaskResume) != 0;
     const bool save = (t.flags & kTaskSaveState) != 0 && p.state != nullptr;
+    // planar row state: strand s of this read at state + state_off + s*m_pad
+    const float *st_plane0 = p.state ? p.state + t.state_off : nullptr;
+    // element offset of this item's strand in a planar FP32 reference
+    const int64_t ref_plane = PREC == 1 && p.ref_layout == 1 ? (int64_t)strand * p.m_pad : 0;
 
     float bestx = __int_as_float(0x7f800000), besty = bestx;
     int64_t colx = -1, coly = -1;
 
-    if (p.use_tma && lane == 0) {
-      mbar_expect_tx(&bars[0], STRIP_BYTES);
+    if (p.use_tma) {
       fence_proxy_async_smem();
-      tma_load_2d(slot0, &tmap, &bars[0], 0, (int)(x0 * PB / 128));
+      tma_issue_if(slot0, &tmap, &bars[0], 0, (int)((ref_plane + x0) * EB / 128), STRIP_BYTES, is0);
     }
 
     for (int s = 0; s < nstrips; ++s) {
@@ -321,17 +391,19 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
 
       // -- initial row ("row -1"): zeros (free start) or the saved row state
       V D[S];
-      float2 O = make_float2(0.f, 0.f);
+      float2 O = make_float2(0.f, 0.f);  // FP16 frame offsets (fwd, rev)
       if (resume) {
-        // two passes over the saved row: strip minimum first (FP16 frame), then the cells
-        const float4 *st = reinterpret_cast<const float4 *>(p.state + t.state_off + x + (int64_t)lane * S);
+        const int64_t c0 = x + (int64_t)lane * S;
         if constexpr (PREC == 0) {
+          // two passes over the saved planes: strip minimum first, then the cells
+          const float4 *f0 = reinterpret_cast<const float4 *>(st_plane0 + c0);
+          const float4 *f1 = reinterpret_cast<const float4 *>(st_plane0 + p.m_pad + c0);
           float mx = __int_as_float(0x7f800000), my = mx;
 #pragma unroll
-          for (int k = 0; k < S / 2; ++k) {
-            const float4 v = st[k];
-            mx = fminf(mx, fminf(v.x, v.z));
-            my = fminf(my, fminf(v.y, v.w));
+          for (int k = 0; k < S / 4; ++k) {
+            const float4 u = f0[k], v = f1[k];
+            mx = fminf(mx, fminf(fminf(u.x, u.y), fminf(u.z, u.w)));
+            my = fminf(my, fminf(fminf(v.x, v.y), fminf(v.z, v.w)));
           }
 #pragma unroll
           for (int m = 16; m >= 1; m >>= 1) {
@@ -339,17 +411,30 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
             my = fminf(my, __shfl_xor_sync(FULL_MASK, my, m));
           }
           O = make_float2(mx, my);
-        }
 #pragma unroll
-        for (int k = 0; k < S / 2; ++k) {
-          const float4 v = st[k];
-          D[2 * k] = P::from_f2(make_float2(v.x - O.x, v.y - O.y));
-          D[2 * k + 1] = P::from_f2(make_float2(v.z - O.x, v.w - O.y));
+          for (int k = 0; k < S / 4; ++k) {
+            const float4 u = f0[k], v = f1[k];
+            D[4 * k] = __floats2half2_rn(u.x - mx, v.x - my);
+            D[4 * k + 1] = __floats2half2_rn(u.y - mx, v.y - my);
+            D[4 * k + 2] = __floats2half2_rn(u.z - mx, v.z - my);
+            D[4 * k + 3] = __floats2half2_rn(u.w - mx, v.w - my);
+          }
+        } else {
+          const float4 *f = reinterpret_cast<const float4 *>(st_plane0 + (int64_t)strand * p.m_pad + c0);
+#pragma unroll
+          for (int k = 0; k < S / 4; ++k) {
+            const float4 u = f[k];
+            D[4 * k] = u.x;
+            D[4 * k + 1] = u.y;
+            D[4 * k + 2] = u.z;
+            D[4 * k + 3] = u.w;
+          }
         }
       } else {
 #pragma unroll
         for (int k = 0; k < S; ++k) D[k] = P::zero();
       }
+
       // -- reference strip into registers (after the row state: fewer live registers)
       V R[S];
       if (p.use_tma) {
@@ -357,34 +442,38 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
         // every lane waits (acquire of the TMA bytes); the give-up decision is warp-uniform
         const bool ok = __all_sync(FULL_MASK, mbar_wait(&bars[sl], (phase >> sl) & 1u));
         if (!ok) {
-          if (lane == 0) atomicOr(p.err, kErrTmaTimeout);
+          atomicOr(p.err, kErrTmaTimeout);  // every lane: same bit
           return;
         }
         phase ^= 1u << sl;
         regs_from_smem<S, PREC>(slot0 + sl * STRIP_BYTES, lane, R);
         __syncwarp();
-        if (s + 1 < nstrips && lane == 0) {
+        if (s + 1 < nstrips) {
           const int ns = (s + 1) & 1;
           fence_proxy_async_smem();
-          mbar_expect_tx(&bars[ns], STRIP_BYTES);
-          tma_load_2d(slot0 + ns * STRIP_BYTES, &tmap, &bars[ns], 0, (int)((x + W) * PB / 128));
+          tma_issue_if(slot0 + ns * STRIP_BYTES, &tmap, &bars[ns], 0, (int)((ref_plane + x + W) * EB / 128),
+                       STRIP_BYTES, is0);
         }
+      } else if constexpr (PREC == 1) {
+        if (p.ref_layout == 0)
+          regs_from_pairs<S>(reinterpret_cast<const float2 *>(p.ref_plain), x, lane, strand, R);
+        else
+          regs_from_global<S, PREC>(reinterpret_cast<const float *>(p.ref_plain) + ref_plane + x, lane, R);
       } else {
-        regs_from_global<S, PREC>(p.ref_plain, x, lane, R);
+        regs_from_global<S, PREC>(reinterpret_cast<const __half2 *>(p.ref_plain) + x, lane, R);
       }
 
-      if (lane == 31) seam_out[0] = D[S - 1];
-      if constexpr (PREC == 0) {
-        if (lane == 0) off_out[0] = O;
-      }
+      // uniform stores (every lane writes the same value): no lane-dependent branch
+      seam_out[0] = P::shfl(D[S - 1], 31);
+      if constexpr (PREC == 0) off_out[0] = O;
 
-      // offset of this strip's frame relative to the left strip's frame
+      // offset of this strip's frame relative to the left strip's frame (FP16)
       V delta = P::zero();
       float2 off_next = make_float2(0.f, 0.f);
       if constexpr (PREC == 0) {
         if (!first) {
           const float2 oi = off_in[0];
-          delta = P::from_f2(make_float2(oi.x - O.x, oi.y - O.y));
+          delta = __float22half2_rn(make_float2(oi.x - O.x, oi.y - O.y));
           if (n >= K) off_next = off_in[1];
         }
       }
@@ -401,11 +490,15 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
         const int r = i0 + kWarp + lane;
         const float qn = r < n ? q[r] : 0.f;
         const V sn = (!first && r < rows) ? seam_in[r] : vinf;
+        // the seam column leaving this strip is gathered in a register window
+        // (lane l keeps row i0+l) and stored once per 32 rows, coalesced: no
+        // lane-conditional store inside the row loop
+        V sout = vinf;
         if (rows - i0 >= kWarp) {
 #pragma unroll 4
           for (int il = 0; il < kWarp; ++il) {
-            sweep_row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), lane);
-            if (lane == 31) so[il] = D[S - 1];
+            sweep_row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+            sout = P::sel(lane == il, P::shfl(D[S - 1], 31), sout);
           }
           if constexpr (PREC == 0) {
             // rescale: subtract this strip's row minimum (one epoch = 32 rows)
@@ -420,18 +513,21 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
             O.x += mf.x;
             O.y += mf.y;
             const int e = (i0 + kWarp) / K;
-            if (lane == 0) off_out[e] = O;
-            if (lane == 31) so[kWarp - 1] = D[S - 1];  // the seam leaves in the new frame
+            off_out[e] = O;  // warp-uniform value, stored by every lane
+            sout = P::sel(lane == kWarp - 1, P::shfl(D[S - 1], 31), sout);  // the seam leaves in the new frame
             if (!first) {
-              delta = P::from_f2(make_float2(off_next.x - O.x, off_next.y - O.y));
+              delta = __float22half2_rn(make_float2(off_next.x - O.x, off_next.y - O.y));
               if ((e + 1) * K <= n) off_next = off_in[e + 1];
             }
           }
+          so[lane] = sout;
         } else {
-          for (int il = 0; il < rows - i0; ++il) {
-            sweep_row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), lane);
-            if (lane == 31) so[il] = D[S - 1];
+          const int cnt = rows - i0;
+          for (int il = 0; il < cnt; ++il) {
+            sweep_row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+            sout = P::sel(lane == il, P::shfl(D[S - 1], 31), sout);
           }
+          so[lane] = sout;  // lanes >= cnt write +inf into the buffer's 32-entry slack past the rows
         }
         so += kWarp;
         qwin = P::qw(qn);
@@ -439,44 +535,64 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
         if constexpr (PREC == 0) swin = __hadd2(swin, delta);
       }
       if (rows < n) {
-        // rows this halo strip skipped can no longer reach column a: keep them inert
-        for (int r = rows + 1 + lane; r <= n; r += kWarp) seam_out[r] = vinf;
+        // rows this halo strip skipped can no longer reach column a: keep them
+        // inert (whole 32-entry groups; the buffers have 32 entries of slack)
+        for (int rr = rows + 1; rr <= n; rr += kWarp) seam_out[rr + lane] = vinf;
         if constexpr (PREC == 0) {
-          for (int e = rows / K + 1 + lane; e <= n / K; e += kWarp) off_out[e] = O;
+          for (int e = rows / K + 1; e <= n / K; e += kWarp) off_out[e + lane] = O;
         }
       }
       __syncwarp();
 
       if (relevant) {
         const int64_t c0 = x + (int64_t)lane * S;
+        if constexpr (PREC == 0) {
 #pragma unroll
-        for (int k = 0; k < S; ++k) {
-          const float2 v = P::to_f2(D[k]);
-          const float vx = v.x + O.x, vy = v.y + O.y;
-          const int64_t col = c0 + k;
-          if (col < b) {
-            if (vx < bestx) { bestx = vx; colx = col; }
-            if (vy < besty) { besty = vy; coly = col; }
+          for (int k = 0; k < S; ++k) {
+            const float2 v = __half22float2(D[k]);
+            const float vx = v.x + O.x, vy = v.y + O.y;
+            const int64_t col = c0 + k;
+            if (col < b) {
+              if (vx < bestx) { bestx = vx; colx = col; }
+              if (vy < besty) { besty = vy; coly = col; }
+            }
           }
-        }
-        if (save) {
-          float2 *st = p.state + t.state_off + c0;
+          if (save) {
+            float4 *f0 = reinterpret_cast<float4 *>(p.state + t.state_off + c0);
+            float4 *f1 = reinterpret_cast<float4 *>(p.state + t.state_off + p.m_pad + c0);
 #pragma unroll
-          for (int k = 0; k < S; k += 2) {
-            const float2 v0 = P::to_f2(D[k]);
-            const float2 v1 = P::to_f2(D[k + 1]);
-            *reinterpret_cast<float4 *>(st + k) =
-                make_float4(v0.x + O.x, v0.y + O.y, v1.x + O.x, v1.y + O.y);
+            for (int k = 0; k < S / 4; ++k) {
+              const float2 v0 = __half22float2(D[4 * k]), v1 = __half22float2(D[4 * k + 1]);
+              const float2 v2 = __half22float2(D[4 * k + 2]), v3 = __half22float2(D[4 * k + 3]);
+              f0[k] = make_float4(v0.x + O.x, v1.x + O.x, v2.x + O.x, v3.x + O.x);
+              f1[k] = make_float4(v0.y + O.y, v1.y + O.y, v2.y + O.y, v3.y + O.y);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < S; ++k) {
+            const int64_t col = c0 + k;
+            if (col < b && D[k] < bestx) { bestx = D[k]; colx = col; }
+          }
+          if (save) {
+            float4 *f = reinterpret_cast<float4 *>(p.state + t.state_off + (int64_t)strand * p.m_pad + c0);
+#pragma unroll
+            for (int k = 0; k < S / 4; ++k) f[k] = make_float4(D[4 * k], D[4 * k + 1], D[4 * k + 2], D[4 * k + 3]);
           }
         }
       }
     }
 
     warp_argmin(bestx, colx);
-    warp_argmin(besty, coly);
-    if (lane == 0) {
-      if (colx >= 0) atomicMin(&p.keys[2 * (int64_t)t.out_slot + 0], make_key(bestx, colx));
-      if (coly >= 0) atomicMin(&p.keys[2 * (int64_t)t.out_slot + 1], make_key(besty, coly));
+    if constexpr (PREC == 0) warp_argmin(besty, coly);
+    {
+      const int64_t base = 2 * (int64_t)t.out_slot;
+      if constexpr (PREC == 0) {
+        red_min_if(&p.keys[base + 0], make_key(bestx, colx), is0 & (colx >= 0 ? 1u : 0u));
+        red_min_if(&p.keys[base + 1], make_key(besty, coly), is0 & (coly >= 0 ? 1u : 0u));
+      } else {
+        red_min_if(&p.keys[base + strand], make_key(bestx, colx), is0 & (colx >= 0 ? 1u : 0u));
+      }
     }
   }
 }
@@ -510,7 +626,7 @@ static int occ_inst(int warps) {
   return n;
 }
 
-int sdtw_pair_bytes(int precision) { return precision == 0 ? 4 : 8; }
+int sdtw_pair_bytes(int precision) { (void)precision; return 4; }
 
 size_t sdtw_smem_bytes(int precision, int cells_per_thread, int warps_per_cta) {
   const size_t strip = (size_t)kWarp * cells_per_thread * sdtw_pair_bytes(precision);
@@ -519,7 +635,7 @@ size_t sdtw_smem_bytes(int precision, int cells_per_thread, int warps_per_cta) {
 
 bool sdtw_instance_exists(int precision, int S) {
   if (precision == 0) return S == 32 || S == 48;
-  return S == 16 || S == 24;
+  return S == 16 || S == 32 || S == 48;
 }
 
 #define DTWX_DISPATCH(PREC, S, CALL) \
@@ -530,7 +646,8 @@ cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, 
   DTWX_DISPATCH(0, 32, launch_inst)(warps_per_cta, grid, p, tmap, s);
   DTWX_DISPATCH(0, 48, launch_inst)(warps_per_cta, grid, p, tmap, s);
   DTWX_DISPATCH(1, 16, launch_inst)(warps_per_cta, grid, p, tmap, s);
-  DTWX_DISPATCH(1, 24, launch_inst)(warps_per_cta, grid, p, tmap, s);
+  DTWX_DISPATCH(1, 32, launch_inst)(warps_per_cta, grid, p, tmap, s);
+  DTWX_DISPATCH(1, 48, launch_inst)(warps_per_cta, grid, p, tmap, s);
   return cudaErrorInvalidValue;
 }
 
@@ -538,7 +655,8 @@ int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta) {
   DTWX_DISPATCH(0, 32, occ_inst)(warps_per_cta);
   DTWX_DISPATCH(0, 48, occ_inst)(warps_per_cta);
   DTWX_DISPATCH(1, 16, occ_inst)(warps_per_cta);
-  DTWX_DISPATCH(1, 24, occ_inst)(warps_per_cta);
+  DTWX_DISPATCH(1, 32, occ_inst)(warps_per_cta);
+  DTWX_DISPATCH(1, 48, occ_inst)(warps_per_cta);
   return 0;
 }
 
@@ -546,6 +664,14 @@ int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta) {
 // Runs only the cell update of the sweep (sub, min, fma over a register row of
 // 32 pairs, next row from the previous one) with no shuffles, seams or memory:
 // the instruction-issue ceiling of the recurrence on this device.
+
+template <int PREC>
+__device__ __forceinline__ typename Pol<PREC>::V probe_value(float a, float b) {
+  if constexpr (PREC == 0)
+    return __floats2half2_rn(a, b);
+  else
+    return a;
+}
 
 template <int PREC>
 __global__ void __launch_bounds__(256) peak_probe_kernel(int iters, float *sink) {
@@ -556,12 +682,12 @@ __global__ void __launch_bounds__(256) peak_probe_kernel(int iters, float *sink)
   const float t = (float)(threadIdx.x & 7) * 0.01f;
 #pragma unroll
   for (int k = 0; k < S; ++k) {
-    R[k] = P::qv(t + 0.03f * k);
+    R[k] = probe_value<PREC>(t + 0.03f * k, t - 0.021f * k);  // distinct strands and columns
     D[k] = P::zero();
   }
   float qf = 0.25f + t;
   for (int it = 0; it < iters; ++it) {
-    const V qq = P::qv(qf);
+    const V qq = probe_value<PREC>(qf, qf);
 #pragma unroll
     for (int k = S - 1; k >= 1; --k) D[k] = P::cell(R[k], qq, D[k], D[k - 1]);
     D[0] = P::cell(R[0], qq, D[0], D[S - 1]);
@@ -571,8 +697,12 @@ __global__ void __launch_bounds__(256) peak_probe_kernel(int iters, float *sink)
   V acc = D[0];
 #pragma unroll
   for (int k = 1; k < S; ++k) acc = P::vmin(acc, D[k]);
-  const float2 f = P::to_f2(acc);
-  if (f.x == 12345.678f) sink[threadIdx.x] = f.y;  // keeps the loop alive
+  float f;
+  if constexpr (PREC == 0)
+    f = __low2float(acc) + __high2float(acc);
+  else
+    f = acc;
+  if (f == 12345.678f) sink[threadIdx.x] = f;  // keeps the loop alive
 }
 
 cudaError_t launch_peak_probe(int precision, int grid, int block, int iters, float *sink,

@@ -209,9 +209,10 @@ int dtwx_last_sweep_ms(dtwx_handle *h, float *ms);
  * at compile time (SEGMENT_SIZE, BLOCK_NUM; src/include/common.hpp:64-79). */
 int dtwx_autotune(dtwx_handle *h, int32_t n_reads, int32_t read_len, float *best_ms);
 
-/* The launch shape of the handle's most recent sweep. */
-int dtwx_get_tuning(const dtwx_handle *h, int32_t *cells_per_thread,
-                    int32_t *chunk_strips, int32_t *warps_per_cta);
+/* Launch shape of the handle's most recent batched sweep in its precision:
+ * out[0..n) = cells per thread, strips per work item, warps per CTA, CTAs,
+ * work items, resident CTAs per SM (as many as n asks for, up to 6). */
+int dtwx_get_tuning(const dtwx_handle *h, int32_t *out, int32_t n);
 
 /* Measured issue-rate ceiling of the cell update on this device: a kernel that
  * runs only the per-cell instruction mix (sub, min, fma) of the given
