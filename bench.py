@@ -288,6 +288,13 @@ def run_ours(args, rank, world, local):
     reads_per_s = world * n_reads * args.steps / (total_ms / 1e3)
     mean_sweep_s = float(np.mean(sweep_ms)) / 1e3
     achieved = cells / mean_sweep_s / 1e9
+    # pipe-bound ceiling from the SM count and the measured SM clock: FP16 cell
+    # pairs cost 2 FMA-pipe instructions that hold the pipe 2 cycles each
+    # (64 cells/SM/cycle); FP32 cells cost 3 issue slots (42.7 cells/SM/cycle)
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    mhz = clock_rec.get("sm_mhz") or 2070.0
+    per_sm_cycle = 64.0 if precision == d.FP16 else 128.0 / 3.0
+    theoretical = sms * per_sm_cycle * mhz * 1e6 / 1e9
     traffic = traffic_from_profile(args.precision)
     t_mask = w.reads.target == 1
     line = {
@@ -303,6 +310,7 @@ def run_ours(args, rank, world, local):
         "reads_per_s": reads_per_s,
         "roofline": {"bound": "alu", "achieved": achieved, "peak": peak / 1e9, "unit": "Gcell/s",
                      "frac": achieved / (peak / 1e9), "traffic": traffic,
+                     "peak_theoretical": theoretical, "frac_of_theoretical": achieved / theoretical,
                      "peak_source": "dtwx_peak_probe: the per-cell instruction mix (sub, min, fma) on "
                                     "register-resident cells, all SMs, measured in this run",
                      "kernel": "dtwx::sdtw_kernel, mean of CUDA events around each launch"},
