@@ -35,8 +35,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD = "C2"
-WORKLOAD_DESC = ("precision-study shape: seeded random 1 Mb genome (999,995 k-mer columns per strand, both strands), "
-                 "2,048 reads x 2,000 samples (1,024 target / 1,024 non-target), dwell geometric mean 9, noise sd 1.8 pA")
+WORKLOAD_DESC = {
+    "C2": ("precision-study shape: seeded random 1 Mb genome (999,995 k-mer columns per strand, both strands), "
+           "2,048 reads x 2,000 samples (1,024 target / 1,024 non-target), dwell geometric mean 9, noise sd 1.8 pA"),
+    "C3": ("batched uneven reads: seeded random 5 Mb genome (4,999,995 k-mer columns per strand, both strands), "
+           "8,192 reads of U[1000, 8000] samples (50/50 target / non-target), one persistent launch, "
+           "CUDA-graph replay, autotuned launch shape"),
+}
 CPU_TARGET_S = 15.0
 
 
@@ -181,7 +186,7 @@ def run_reference(args, rank, world):
     from dtwax_gb300 import synth
     if rank != 0:
         return 0
-    w = synth.make_workload(WORKLOAD)
+    w = synth.make_workload(args.workload)
     # each step is one pass over the bounded sample; warm-up passes are shorter
     cpu_baseline(w, 1, target_s=2.0) if args.warmup > 0 else None
     rec = cpu_baseline(w, n_steps=max(args.steps, 1), target_s=max(4.0, 60.0 / max(args.steps, 1)))
@@ -189,7 +194,7 @@ def run_reference(args, rank, world):
             "warmup": args.warmup, "ms_per_step": rec["seconds"] * 1e3 / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"{WORKLOAD}: {WORKLOAD_DESC}", "implementation":
+            "config": {"workload": f"{args.workload}: {WORKLOAD_DESC[args.workload]}", "implementation":
                        "oracle/sdtw_oracle.c: OpenMP FP64 restatement of scripts/sdtw.py sdtw_default "
                        "(numba original not installed); bounded read sample"},
             "cpu_baseline": {k: rec[k] for k in ("value", "unit", "cores", "kind", "sample")},
@@ -223,14 +228,16 @@ def run_ours(args, rank, world, local):
         return float(t.item())
 
     precision = d.FP16 if args.precision == "fp16" else d.FP32
-    w = synth.make_workload(WORKLOAD, n_reads=args.reads or None)
+    w = synth.make_workload(args.workload, n_reads=args.reads or None)
     cells = w.cells()
     n_reads = w.reads.n
     peak = d.peak_probe(local, precision, 400.0)
+    use_graphs = 1 if (args.graphs or args.workload == "C3") else 0
     clf = d.Classifier(sequence=w.genome, level_table=w.table, precision=precision, device=local,
-                       cells_per_thread=args.cells, chunk_strips=args.strips, warps_per_cta=args.warps)
-    if args.autotune:
-        clf.autotune(n_reads, int(np.diff(w.reads.offsets).max()))
+                       cells_per_thread=args.cells, chunk_strips=args.strips, warps_per_cta=args.warps,
+                       use_graphs=use_graphs)
+    if args.autotune or args.workload == "C3":
+        clf.autotune(n_reads, int(np.diff(w.reads.offsets).mean()))
     stream = torch.cuda.Stream()
     d_raw = torch.tensor(w.reads.raw, device="cuda")
     d_out = torch.zeros(32 * n_reads, dtype=torch.uint8, device="cuda")
@@ -269,7 +276,7 @@ def run_ours(args, rank, world, local):
 
     # end to end through the public host API: host samples in, results out
     e2e_ms = []
-    for _ in range(max(2, min(args.steps, 5))):
+    for _ in range(max(1 if args.workload == "C3" else 2, min(args.steps, 5))):
         t = time.perf_counter()
         host_res = clf.classify(raw=w.reads.raw, offsets=w.reads.offsets)
         e2e_ms.append((time.perf_counter() - t) * 1e3)
@@ -302,7 +309,7 @@ def run_ours(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f16x2" if precision == d.FP16 else "f32",
         "data": "synthetic",
-        "config": {"workload": f"{WORKLOAD}: {WORKLOAD_DESC}", "cells_per_step": cells,
+        "config": {"workload": f"{args.workload}: {WORKLOAD_DESC[args.workload]}", "cells_per_step": cells,
                    "reads_per_step": n_reads, "ref_columns_per_strand": w.ref_len,
                    "precision": args.precision, "step": "window+z-score kernel, sDTW sweep, min/argmin finalize; "
                    "raw samples resident in HBM", "l2": "flushed between timed steps (256 MB write)",
@@ -355,6 +362,9 @@ def main():
     ap.add_argument("--strips", type=int, default=0, help="strips per work item (0 = tuned)")
     ap.add_argument("--warps", type=int, default=0, help="warps per CTA (0 = tuned)")
     ap.add_argument("--autotune", action="store_true", help="time candidate launch shapes before measuring")
+    ap.add_argument("--graphs", action="store_true", help="replay the step as a captured CUDA graph")
+    ap.add_argument("--workload", choices=["C2", "C3"], default=WORKLOAD,
+                    help="C2: 2,048 x 2,000 samples vs 1 Mb (default); C3: 8,192 uneven reads vs 5 Mb")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

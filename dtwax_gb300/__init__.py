@@ -46,7 +46,7 @@ class Config(ctypes.Structure):
         ("norm_eps", ctypes.c_float), ("threshold", ctypes.c_float),
         ("max_batch_reads", ctypes.c_int32), ("cells_per_thread", ctypes.c_int32),
         ("chunk_strips", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 8),
+        ("use_graphs", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7),
     ]
 
 
@@ -302,9 +302,10 @@ class Classifier:
 
     def tuning(self):
         """Launch shape of the most recent batched sweep."""
-        v = (ctypes.c_int32 * 6)()
-        _check(self._lib.dtwx_get_tuning(self._h, v, 6), self._h)
-        keys = ("cells_per_thread", "chunk_strips", "warps_per_cta", "ctas", "work_items", "ctas_per_sm")
+        v = (ctypes.c_int32 * 7)()
+        _check(self._lib.dtwx_get_tuning(self._h, v, 7), self._h)
+        keys = ("cells_per_thread", "chunk_strips", "warps_per_cta", "ctas", "work_items", "ctas_per_sm",
+                "graph_replays")
         return dict(zip(keys, list(v)))
 
     # -- Read Until serving

@@ -96,6 +96,12 @@ struct dtwx_handle {
   };
   std::map<std::tuple<int, int, int>, Tuned> tuned;
   Shape override_shape;      // set while the autotuner times a candidate
+  // CUDA graph of the most recent repeated device batch
+  uint64_t graph_key = 0, graph_pending = 0;
+  cudaGraphExec_t graph_exec = nullptr;
+  int32_t graph_launches = 0;
+  int64_t graph_replays = 0;
+  bool capturing = false;
   BatchCtx ctx[3];           // [0] offline calls, [1] and [2] the two serving batches
   std::string err;
   int32_t last_launches = 0;
@@ -128,6 +134,13 @@ int fail(dtwx_handle *h, int code, const std::string &msg) {
     g_create_err = msg;
   return code;
 }
+
+// Ends a stream capture that an error left open, so the caller's stream stays usable.
+struct CaptureGuard {
+  dtwx_handle *h;
+  cudaStream_t st;
+  ~CaptureGuard();
+};
 
 #define CK(h, call)                                                                         \
   do {                                                                                      \
@@ -294,10 +307,12 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
     p.strands = strands;
     const int ii = inst_index(precision, sh.S);
     p.use_tma = h->tmap_ok[precision][ii] ? 1 : 0;
-    CK(h, cudaEventRecord(c.sweep_beg, st));
+    // inside a stream capture the timing events become event-record nodes
+    const unsigned ev_flags = h->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    CK(h, cudaEventRecordWithFlags(c.sweep_beg, st, ev_flags));
     CK(h, launch_sdtw(precision, sh.S, sh.warps, sh.grid, p, p.use_tma ? &h->tmap[precision][ii] : nullptr,
                       st));
-    CK(h, cudaEventRecord(c.sweep_end, st));
+    CK(h, cudaEventRecordWithFlags(c.sweep_end, st, ev_flags));
     c.sweep_timed = true;
     ++launches;
   }
@@ -440,6 +455,41 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
     if (is_i16 && sc_range && sc_digi) smul[r] = sc_digi[r] != 0.f ? sc_range[r] / sc_digi[r] : 1.f;
     if (is_i16 && sc_off) sadd[r] = sc_off[r];
   }
+  // ---- CUDA graph of a repeated device batch
+  CaptureGuard capture_guard{h, st};
+  const bool graphable = h->cfg.use_graphs && raw_dev && out_dev && !raw_host && !one_launch_per_read;
+  uint64_t key = 0;
+  if (graphable) {
+    uint64_t hsh = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) {
+      for (int i = 0; i < 8; ++i) {
+        hsh ^= (v >> (8 * i)) & 0xff;
+        hsh *= 1099511628211ull;
+      }
+    };
+    mix(reinterpret_cast<uintptr_t>(raw_dev));
+    mix(reinterpret_cast<uintptr_t>(out_dev));
+    mix(reinterpret_cast<uintptr_t>(st));
+    mix((uint64_t)n_reads);
+    mix((uint64_t)precision);
+    for (int r = 0; r <= n_reads; ++r) mix((uint64_t)offsets[r]);
+    key = hsh | 1;
+    if (key == h->graph_key && h->graph_exec) {
+      // the pinned metadata blob was refilled above; the graph's copy reads it at replay
+      CK(h, cudaGraphLaunch(h->graph_exec, st));
+      CK(h, cudaEventRecord(c.meta_free, st));
+      c.meta_pending = true;
+      h->last_launches = h->graph_launches;
+      ++h->graph_replays;
+      return DTWX_OK;
+    }
+    if (key == h->graph_pending) {
+      CK(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      h->capturing = true;
+    } else {
+      h->graph_pending = key;
+    }
+  }
   const void *src_dev = raw_dev;
   if (raw_host) {
     CK(h, c.h_raw.ensure(std::max<size_t>(es * (size_t)w.total, 16)));
@@ -452,8 +502,10 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
     src_dev = c.raw.p;
   }
   CK(h, cudaMemcpyAsync(c.meta.p, c.h_meta.p, L.total, cudaMemcpyHostToDevice, st));
-  CK(h, cudaEventRecord(c.meta_free, st));
-  c.meta_pending = true;
+  if (!h->capturing) {
+    CK(h, cudaEventRecord(c.meta_free, st));
+    c.meta_pending = true;
+  }
   const char *dm = c.meta.as<char>();
   CK(h, c.query.ensure(sizeof(float) * (size_t)std::max<int64_t>(w.total, 4)));
   CK(h, c.results.ensure(sizeof(dtwx_result) * (size_t)std::max(n_reads, 1)));
@@ -528,6 +580,22 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
     ++launches;
   }
   h->last_launches = launches;
+  if (h->capturing) {
+    h->capturing = false;
+    cudaGraph_t graph = nullptr;
+    CK(h, cudaStreamEndCapture(st, &graph));
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(h, ie);
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    h->graph_exec = exec;
+    h->graph_key = key;
+    h->graph_launches = launches;
+    CK(h, cudaGraphLaunch(exec, st));
+    CK(h, cudaEventRecord(c.meta_free, st));
+    c.meta_pending = true;
+  }
   if (out_host) {
     if (n_reads)
       CK(h, cudaMemcpyAsync(out_host, d_out, sizeof(dtwx_result) * (size_t)n_reads, cudaMemcpyDeviceToHost, st));
@@ -631,6 +699,16 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
 
 void dtwx::set_create_error(const char *msg) { g_create_err = msg ? msg : ""; }
 
+CaptureGuard::~CaptureGuard() {
+  if (h && h->capturing) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(st, &g);
+    if (g) cudaGraphDestroy(g);
+    h->capturing = false;
+    h->graph_pending = 0;
+  }
+}
+
 // =================================================================== C ABI
 
 extern "C" {
@@ -720,6 +798,7 @@ int dtwx_destroy(dtwx_handle *h) {
     if (c.done) cudaEventDestroy(c.done);
     if (c.stream) cudaStreamDestroy(c.stream);
   }
+  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
   h->ref16.release();
   h->ref32.release();
   h->fwd32.release();
@@ -824,10 +903,14 @@ int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets,
   return rc;
 }
 
-int dtwx_autotune(dtwx_handle *h, int32_t n_reads, int32_t read_len, float *best_ms) {
-  if (!h || n_reads <= 0 || read_len <= 0) return DTWX_E_ARG;
+int dtwx_autotune(dtwx_handle *h, int32_t n_reads_req, int32_t read_len, float *best_ms) {
+  if (!h || n_reads_req <= 0 || read_len <= 0) return DTWX_E_ARG;
   CK(h, cudaSetDevice(h->device));
   const int prec = h->cfg.precision;
+  // candidates are timed on at most 1024 reads; the winner is kept for the
+  // requested batch size (its chunk width is a factor on the analytic model,
+  // which rescales with the batch)
+  const int32_t n_reads = std::min<int32_t>(n_reads_req, 1024);
   // synthetic z-scored reads of the requested shape (the sweep's cost does not
   // depend on the sample values)
   std::vector<float> q((size_t)n_reads * read_len);
@@ -874,8 +957,9 @@ int dtwx_autotune(dtwx_handle *h, int32_t n_reads, int32_t read_len, float *best
   h->override_shape = Shape{};
   if (rc != DTWX_OK) return rc;
   CK(h, cudaStreamSynchronize(st));
-  h->tuned[std::make_tuple(prec, log2_bucket(n_reads), log2_bucket(read_len))] =
-      dtwx_handle::Tuned{win.S, win.warps, win.permille / 1000.0};
+  const dtwx_handle::Tuned tw{win.S, win.warps, win.permille / 1000.0};
+  h->tuned[std::make_tuple(prec, log2_bucket(n_reads_req), log2_bucket(read_len))] = tw;
+  h->tuned[std::make_tuple(prec, log2_bucket(n_reads), log2_bucket(read_len))] = tw;
   if (best_ms) *best_ms = best;
   return DTWX_OK;
 }
@@ -894,8 +978,9 @@ int dtwx_last_sweep_ms(dtwx_handle *h, float *ms) {
 int dtwx_get_tuning(const dtwx_handle *h, int32_t *out, int32_t n) {
   if (!h || !out || n < 0) return DTWX_E_ARG;
   const Shape &s = h->last_shape[h->cfg.precision];
-  const int32_t v[6] = {s.S, s.G, s.warps, s.grid, s.items, s.S ? sdtw_ctas_per_sm(h->cfg.precision, s.S, s.warps) : 0};
-  for (int i = 0; i < n && i < 6; ++i) out[i] = v[i];
+  const int32_t v[7] = {s.S, s.G, s.warps, s.grid, s.items,
+                        s.S ? sdtw_ctas_per_sm(h->cfg.precision, s.S, s.warps) : 0, (int32_t)h->graph_replays};
+  for (int i = 0; i < n && i < 7; ++i) out[i] = v[i];
   return DTWX_OK;
 }
 

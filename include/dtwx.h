@@ -66,7 +66,10 @@ typedef struct dtwx_config {
   int32_t cells_per_thread;/* DP columns per lane; 0 = autotune */
   int32_t chunk_strips;    /* strips (32 lanes x cells_per_thread columns) per work item; 0 = autotune */
   int32_t warps_per_cta;   /* 0 = autotune */
-  int32_t reserved[8];
+  int32_t use_graphs;      /* 1: dtwx_classify_device replays a captured CUDA graph when a batch
+                              repeats (same buffers, offsets and stream): the first such batch runs
+                              directly, the second is captured, later ones are replays */
+  int32_t reserved[7];
 } dtwx_config;
 
 /* Per-read outcome.  end_pos is the DP column (0-based k-mer position on the
@@ -201,17 +204,18 @@ int32_t dtwx_last_launch_count(const dtwx_handle *h);
  * figure with TIMERSTOP_CUDA (src/include/hpc_helpers.hpp:93-100). */
 int dtwx_last_sweep_ms(dtwx_handle *h, float *ms);
 
-/* Autotuner: time the sweep on a synthetic batch of n_reads reads of
- * read_len samples for every compiled cells-per-thread instance, 4 and 8 warps
- * per CTA, and half / once / twice the analytic chunk width; the fastest shape
- * is used from then on for batches of that size (log2 buckets of read count
- * and read length).  *best_ms gets its sweep time.  The reference fixes these
+/* Autotuner: time the sweep on a synthetic batch of min(n_reads, 1024) reads
+ * of read_len samples for every compiled cells-per-thread instance, 4 and 8
+ * warps per CTA, and half / once / twice the analytic chunk width; the fastest
+ * shape is used from then on for batches of n_reads reads of that length (log2
+ * buckets of read count and read length).  *best_ms gets its sweep time.  The reference fixes these
  * at compile time (SEGMENT_SIZE, BLOCK_NUM; src/include/common.hpp:64-79). */
 int dtwx_autotune(dtwx_handle *h, int32_t n_reads, int32_t read_len, float *best_ms);
 
 /* Launch shape of the handle's most recent batched sweep in its precision:
  * out[0..n) = cells per thread, strips per work item, warps per CTA, CTAs,
- * work items, resident CTAs per SM (as many as n asks for, up to 6). */
+ * work items, resident CTAs per SM, CUDA-graph replays so far (as many as n
+ * asks for, up to 7). */
 int dtwx_get_tuning(const dtwx_handle *h, int32_t *out, int32_t n);
 
 /* Measured issue-rate ceiling of the cell update on this device: a kernel that

@@ -289,3 +289,30 @@ def test_autotune_picks_a_compiled_shape_and_keeps_results(lib, genome_pair):
     assert ms > 0
     assert t["cells_per_thread"] in (16, 32, 48) and t["warps_per_cta"] in (4, 8) and t["ctas_per_sm"] >= 1
     np.testing.assert_array_equal(after["score"], before["score"])  # FP32: shape never changes the bits
+
+
+def test_cuda_graph_replay_matches_direct_launches(lib, genome_pair):
+    """A repeated device batch runs directly once, is captured the second
+    time and replayed afterwards; every call returns the same results."""
+    import torch
+    import dtwax_gb300 as d
+    g, o = genome_pair
+    tab = synth.level_table()
+    reads = reads_of_lengths(g, o, tab, [2000, 1200, 4000, 33, 1])
+    with make_classifier(g, tab, precision=0, use_graphs=1) as clf:
+        host = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        stream = torch.cuda.Stream()
+        draw = torch.tensor(reads.raw, device="cuda")
+        dout = torch.zeros(32 * reads.n, dtype=torch.uint8, device="cuda")
+        got = []
+        for _ in range(4):
+            dout.zero_()
+            torch.cuda.synchronize()
+            clf.classify_device(draw.data_ptr(), reads.offsets, dout.data_ptr(), stream.cuda_stream)
+            stream.synchronize()
+            got.append(np.frombuffer(dout.cpu().numpy().tobytes(), d.RESULT_DTYPE).copy())
+            assert clf.last_sweep_ms() > 0
+        assert clf.tuning()["graph_replays"] == 2
+    for r in got:
+        np.testing.assert_array_equal(r["score"], host["score"])
+        np.testing.assert_array_equal(r["end_pos"], host["end_pos"])
