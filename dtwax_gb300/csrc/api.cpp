@@ -944,10 +944,8 @@ int dtwx_autotune(dtwx_handle *h, int32_t n_reads_req, int32_t read_len, float *
     h->override_shape.warps = cd.warps;
     h->override_shape.items = cd.permille;
     float ms = 0.f;
-    for (int rep = 0; rep < 2 && rc == DTWX_OK; ++rep) {  // first run warms this shape up
-      rc = dtwx_distances(h, dq.as<float>(), offs.data(), n_reads, dout.as<dtwx_result>(), st);
-      if (rc == DTWX_OK) rc = dtwx_last_sweep_ms(h, &ms);
-    }
+    rc = dtwx_distances(h, dq.as<float>(), offs.data(), n_reads, dout.as<dtwx_result>(), st);
+    if (rc == DTWX_OK) rc = dtwx_last_sweep_ms(h, &ms);
     if (rc != DTWX_OK) break;
     if (ms < best) {
       best = ms;
