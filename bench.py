@@ -328,8 +328,8 @@ def run_ours(args, rank, world, local):
         "clocks": clock_rec,
         "plain_fp32": {"reads_per_s": plain_rps, "sample_reads": n_plain,
                        "speedup_reads_per_s": reads_per_s / world / plain_rps},
-        "check": {"target_score_max": float(res["score"][t_mask].max()),
-                  "other_score_min": float(res["score"][~t_mask].min())},
+        "check": {"target_score_per_sample_max": float((res["score"] / res["n_samples"])[t_mask].max()),
+                  "other_score_per_sample_min": float((res["score"] / res["n_samples"])[~t_mask].min())},
     }
     if args.serving != "none" and rank == 0:
         line["serving"] = run_serving(args.serving, precision, local, args.serving_seconds)

@@ -324,7 +324,9 @@ class Classifier:
         return _check(self._lib.dtwx_serve_step(self._h), self._h)
 
     def poll_decisions(self, cap: int = 4096):
-        buf = (Decision * cap)()
+        buf = getattr(self, "_dbuf", None)
+        if buf is None or len(buf) < cap:
+            buf = self._dbuf = (Decision * cap)()
         n = _check(self._lib.dtwx_poll_decisions(self._h, buf, cap), self._h)
         return [{f: getattr(buf[i], f) for f, _ in Decision._fields_} for i in range(n)]
 

@@ -122,6 +122,9 @@ def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget
     measured-window statistics."""
     from . import now_ms
 
+    # serving batches hold a few chunk-steps each: tune the launch shape for them
+    for k in (1, 2, 4):
+        clf.autotune(k, cfg.chunk)
     clf.serve_start(max_in_flight=max_in_flight, state_budget_bytes=state_budget_bytes,
                     chunks_per_decision=cfg.chunks_per_read, accept_per_sample=accept, reject_per_sample=reject)
     seq = SimulatedSequencer(reads, cfg)
@@ -147,7 +150,7 @@ def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget
                     lat.append(d["latency_ms"])
                     calls.append(d["call"])
                     truth.append(seq.truth.get(d["read_number"], -1))
-        time.sleep(0.0002)
+        time.sleep(0.00005)
     clf.serve_drain()
     st = clf.stats()
     lat = np.asarray(lat)
@@ -164,6 +167,9 @@ def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget
         "call_accuracy": acc,
         "mean_batch_reads": st["mean_batch_reads"], "batches": st["batches"],
         "reads_deferred": st["reads_deferred"], "max_in_flight": st["max_in_flight"],
+        "reads_started": seq.next_read - 1,
+        "deferred_fraction": st["reads_deferred"] / max(seq.next_read - 1, 1),
+        "queue_depth_end": st["queue_depth"],
         "state_bytes": st["state_bytes"],
         "accept_per_sample": accept, "reject_per_sample": reject,
     }

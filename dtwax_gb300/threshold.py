@@ -28,8 +28,14 @@ def parse_log(text_or_lines) -> np.ndarray:
     return np.asarray(scores, np.float64)
 
 
-def best_threshold(target_scores, other_scores, num: int = 100000):
-    """(threshold, accuracy %) maximising (#target < t + #other >= t) / total."""
+def best_threshold(target_scores, other_scores, num: int = 100000, plateau: str = "first"):
+    """(threshold, accuracy %) maximising (#target < t + #other >= t) / total.
+
+    plateau="first" keeps the reference's choice (the first threshold of
+    maximal accuracy, which sits on the edge of the target scores when the
+    classes separate); plateau="center" takes the middle of the run of
+    maximal-accuracy thresholds that contains the first one, which leaves the
+    same margin to both classes."""
     t_s = np.asarray(target_scores, np.float64)
     o_s = np.asarray(other_scores, np.float64)
     if t_s.size + o_s.size == 0:
@@ -41,6 +47,11 @@ def best_threshold(target_scores, other_scores, num: int = 100000):
     correct = np.searchsorted(ts, th, side="left") + (os_.size - np.searchsorted(os_, th, side="left"))
     acc = correct * 100.0 / (t_s.size + o_s.size)
     k = int(np.argmax(acc))
+    if plateau == "center":
+        e = k
+        while e + 1 < acc.size and acc[e + 1] == acc[k]:
+            e += 1
+        return float(0.5 * (th[k] + th[e])), float(acc[k])
     return float(th[k]), float(acc[k])
 
 
