@@ -117,9 +117,10 @@ class SimulatedSequencer:
 
 
 def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget_bytes: float = 0.0,
-        max_in_flight: int = 0) -> dict:
+        max_in_flight: int = 0, drain: bool = False) -> dict:
     """Real-time serving loop for warmup + duration seconds.  Returns the
-    measured-window statistics."""
+    measured-window statistics.  Work still queued at the end is dropped
+    unless `drain` (an overloaded configuration can hold minutes of it)."""
     from . import now_ms
 
     # serving batches hold a few chunk-steps each: tune the launch shape for them
@@ -151,8 +152,9 @@ def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget
                     calls.append(d["call"])
                     truth.append(seq.truth.get(d["read_number"], -1))
         time.sleep(0.00005)
-    clf.serve_drain()
     st = clf.stats()
+    if drain:
+        clf.serve_drain()
     lat = np.asarray(lat)
     calls = np.asarray(calls)
     truth = np.asarray(truth)
