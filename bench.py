@@ -162,7 +162,7 @@ SERVING = {
 }
 
 
-def run_serving(name: str, precision: int, device: int, duration_s: float):
+def run_serving(name: str, precision: int, device: int, duration_s: float, batches: int = 0):
     import dtwax_gb300 as d
     from dtwax_gb300 import readuntil, synth
 
@@ -172,7 +172,8 @@ def run_serving(name: str, precision: int, device: int, duration_s: float):
     tab = synth.level_table()
     cfg = readuntil.ServeConfig(channels=spec["channels"], duration_s=duration_s, warmup_s=2.0)
     reads = readuntil.make_pool(g, o, tab, cfg)
-    with d.Classifier(sequence=g, level_table=tab, precision=precision, device=device) as clf:
+    with d.Classifier(sequence=g, level_table=tab, precision=precision, device=device,
+                      serve_batches=batches) as clf:
         accept, reject = readuntil.calibrate(clf, reads, cfg)
         rec = readuntil.run(clf, reads, cfg, accept, reject, state_budget_bytes=spec["budget_gb"] * 1e9)
     rec["workload"] = (f"{name}: {spec['channels']} channels, 1,600-sample chunks every 0.4 s, Poisson read "
@@ -332,7 +333,7 @@ def run_ours(args, rank, world, local):
                   "other_score_per_sample_min": float((res["score"] / res["n_samples"])[~t_mask].min())},
     }
     if args.serving != "none" and rank == 0:
-        line["serving"] = run_serving(args.serving, precision, local, args.serving_seconds)
+        line["serving"] = run_serving(args.serving, precision, local, args.serving_seconds, args.serve_batches)
     if args.reads:
         line["config"]["workload"] += f" (first {n_reads} reads only)"
     if rank == 0:
@@ -358,6 +359,7 @@ def main():
     ap.add_argument("--serving", choices=["none", "C4", "C5"], default="C4",
                     help="Read Until serving simulation reported beside the batch metric")
     ap.add_argument("--serving-seconds", type=float, default=6.0)
+    ap.add_argument("--serve-batches", type=int, default=0, help="serving batches in flight (0 = library default)")
     ap.add_argument("--cells", type=int, default=0, help="cells per thread (0 = tuned)")
     ap.add_argument("--strips", type=int, default=0, help="strips per work item (0 = tuned)")
     ap.add_argument("--warps", type=int, default=0, help="warps per CTA (0 = tuned)")

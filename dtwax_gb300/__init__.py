@@ -46,7 +46,7 @@ class Config(ctypes.Structure):
         ("norm_eps", ctypes.c_float), ("threshold", ctypes.c_float),
         ("max_batch_reads", ctypes.c_int32), ("cells_per_thread", ctypes.c_int32),
         ("chunk_strips", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
-        ("use_graphs", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7),
+        ("use_graphs", ctypes.c_int32), ("serve_batches", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6),
     ]
 
 
@@ -69,7 +69,8 @@ class Stats(ctypes.Structure):
                 ("queue_depth", ctypes.c_int32), ("in_flight", ctypes.c_int32),
                 ("max_in_flight", ctypes.c_int32), ("batches", ctypes.c_int32),
                 ("p50_latency_ms", ctypes.c_double), ("p99_latency_ms", ctypes.c_double),
-                ("mean_batch_reads", ctypes.c_double), ("state_bytes", ctypes.c_double)]
+                ("mean_batch_reads", ctypes.c_double), ("state_bytes", ctypes.c_double),
+                ("mean_batch_ms", ctypes.c_double), ("max_batch_ms", ctypes.c_double)]
 
 
 # numpy view of dtwx_result (32 bytes)

@@ -31,7 +31,8 @@ namespace {
 
 thread_local std::string g_create_err;
 
-constexpr int64_t kPadCols = 3072;  // a multiple of every compiled strip width (512, 768, 1024, 1536)
+constexpr int64_t kPadCols = 3072;
+constexpr int kServeSlots = 4;      // most serving batches in flight at once, each on its own stream  // a multiple of every compiled strip width (512, 768, 1024, 1536)
 
 struct Shape {
   int S = 0;      // cells (column pairs) per lane
@@ -102,7 +103,7 @@ struct dtwx_handle {
   int32_t graph_launches = 0;
   int64_t graph_replays = 0;
   bool capturing = false;
-  BatchCtx ctx[3];           // [0] offline calls, [1] and [2] the two serving batches
+  BatchCtx ctx[1 + kServeSlots];  // [0] offline calls, [1..] the serving batches
   std::string err;
   int32_t last_launches = 0;
   Shape last_shape[2];
@@ -117,12 +118,13 @@ struct dtwx_handle {
   std::deque<std::pair<int32_t, uint64_t>> admit_queue;
   std::vector<dtwx_decision> decisions;
   std::vector<double> latencies;
-  std::vector<ServeTask> inflight[2];  // tasks of the serving batch in ctx[1 + s]
-  bool running[2] = {false, false};
+  std::vector<ServeTask> inflight[kServeSlots];  // tasks of the serving batch in ctx[1 + s]
+  bool running[kServeSlots] = {};
   float accept_per_sample = 0.f, reject_per_sample = 0.f;
   int64_t chunks_submitted = 0, chunks_processed = 0, reads_decided = 0, reads_deferred = 0;
   int32_t batches = 0;
   double batch_reads_sum = 0;
+  double batch_ms_sum = 0, batch_ms_max = 0;  // device time of the serving sweeps
 };
 
 namespace {
@@ -1130,7 +1132,18 @@ void release_read(dtwx_handle *h, std::map<std::pair<int32_t, uint64_t>, ServeRe
 int harvest(dtwx_handle *h, int slot) {
   BatchCtx &c = h->ctx[1 + slot];
   CK(h, cudaEventSynchronize(c.done));
-  if (int rc = check_device_flags(h, c)) return rc;
+  const int32_t dev_err = c.h_flags.as<int32_t>()[4];
+  if (dev_err) {
+    CK(h, cudaMemset(c.flags.as<int32_t>() + 4, 0, sizeof(int32_t)));
+    return fail(h, (dev_err & kErrTmaTimeout) ? DTWX_E_TIMEOUT : DTWX_E_CAPACITY, "device error flag in a serving batch");
+  }
+  if (c.sweep_timed) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c.sweep_beg, c.sweep_end) == cudaSuccess) {
+      h->batch_ms_sum += ms;
+      h->batch_ms_max = std::max<double>(h->batch_ms_max, ms);
+    }
+  }
   const dtwx_result *res = c.h_results.as<dtwx_result>();
   const double t = now_ms();
   std::vector<ServeTask> &inflight = h->inflight[slot];
@@ -1171,7 +1184,7 @@ int harvest(dtwx_handle *h, int slot) {
 
 // Harvest every serving batch that has finished; `wait` blocks for running ones.
 int harvest_done(dtwx_handle *h, bool wait) {
-  for (int s = 0; s < 2; ++s) {
+  for (int s = 0; s < kServeSlots; ++s) {
     if (!h->running[s]) continue;
     if (!wait) {
       const cudaError_t q = cudaEventQuery(h->ctx[1 + s].done);
@@ -1190,11 +1203,15 @@ int dtwx_serve_step(dtwx_handle *h) {
   if (!h->serving) return fail(h, DTWX_E_STATE, "call dtwx_serve_start first");
   CK(h, cudaSetDevice(h->device));
   if (int rc = harvest_done(h, false)) return rc;
-  // Continuous batching: up to two batches are in flight, each on its own
-  // stream with its own scratch; a new batch starts as soon as a slot is free,
-  // so chunks that arrive while a batch runs reach the GPU without waiting for
-  // it to end.  A read is in at most one batch at a time (its row state).
-  const int slot = !h->running[0] ? 0 : (!h->running[1] ? 1 : -1);
+  // Continuous batching: up to kServeSlots batches are in flight, each on its
+  // own stream with its own scratch; a new batch starts as soon as a slot is
+  // free, so chunks that arrive while batches run reach the GPU without
+  // waiting for them to end.  A read is in at most one batch at a time (its
+  // row state).
+  int slot = -1;
+  const int slots = h->cfg.serve_batches > 0 ? std::min(h->cfg.serve_batches, kServeSlots) : 2;
+  for (int s = 0; s < slots && slot < 0; ++s)
+    if (!h->running[s]) slot = s;
   if (slot < 0) return 0;
   BatchCtx &c = h->ctx[1 + slot];
   // decided reads whose remaining chunks are moot are dropped at decision time;
@@ -1269,6 +1286,8 @@ int dtwx_serve_step(dtwx_handle *h) {
                              launches))
     return rc;
   CK(h, cudaMemcpyAsync(c.h_results.p, c.results.p, sizeof(dtwx_result) * nb, cudaMemcpyDeviceToHost, st));
+  CK(h, c.h_flags.ensure(64));
+  CK(h, cudaMemcpyAsync(c.h_flags.p, c.flags.p, 64, cudaMemcpyDeviceToHost, st));  // read at harvest
   CK(h, cudaEventRecord(c.done, st));
   h->inflight[slot] = batch;
   h->running[slot] = true;
@@ -1294,7 +1313,9 @@ int dtwx_serve_drain(dtwx_handle *h) {
     if (int rc = harvest_done(h, true)) return rc;
     const int rc = dtwx_serve_step(h);
     if (rc < 0) return rc;
-    if (rc == 0 && !h->running[0] && !h->running[1]) break;
+    bool any = false;
+    for (int s = 0; s < kServeSlots; ++s) any |= h->running[s];
+    if (rc == 0 && !any) break;
   }
   return DTWX_OK;
 }
@@ -1313,6 +1334,8 @@ int dtwx_stats_get(dtwx_handle *h, dtwx_stats *out) {
   out->max_in_flight = h->max_in_flight;
   out->batches = h->batches;
   out->mean_batch_reads = h->batches ? h->batch_reads_sum / h->batches : 0.0;
+  out->mean_batch_ms = h->batches ? h->batch_ms_sum / h->batches : 0.0;
+  out->max_batch_ms = h->batch_ms_max;
   out->state_bytes = (double)h->state.cap;
   if (!h->latencies.empty()) {
     std::vector<double> v = h->latencies;

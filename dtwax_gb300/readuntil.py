@@ -168,6 +168,7 @@ def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget
         "max_latency_ms": float(lat.max()) if lat.size else None,
         "call_accuracy": acc,
         "mean_batch_reads": st["mean_batch_reads"], "batches": st["batches"],
+        "mean_batch_ms": st["mean_batch_ms"], "max_batch_ms": st["max_batch_ms"],
         "reads_deferred": st["reads_deferred"], "max_in_flight": st["max_in_flight"],
         "reads_started": seq.next_read - 1,
         "deferred_fraction": st["reads_deferred"] / max(seq.next_read - 1, 1),

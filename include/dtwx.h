@@ -69,7 +69,8 @@ typedef struct dtwx_config {
   int32_t use_graphs;      /* 1: dtwx_classify_device replays a captured CUDA graph when a batch
                               repeats (same buffers, offsets and stream): the first such batch runs
                               directly, the second is captured, later ones are replays */
-  int32_t reserved[7];
+  int32_t serve_batches;   /* serving batches in flight at once (1..4), 0 = 2 */
+  int32_t reserved[6];
 } dtwx_config;
 
 /* Per-read outcome.  end_pos is the DP column (0-based k-mer position on the
@@ -256,6 +257,8 @@ typedef struct dtwx_stats {
   double p99_latency_ms;
   double mean_batch_reads;
   double state_bytes;        /* device bytes of the row-state pool */
+  double mean_batch_ms;      /* device time of a serving batch's sweep, mean and max */
+  double max_batch_ms;
 } dtwx_stats;
 
 /* Prepare the handle for serving.  max_in_flight = reads holding device row
@@ -277,8 +280,8 @@ int dtwx_submit_chunk(dtwx_handle *h, int32_t channel, uint64_t read_number,
                       const float *samples, int32_t n, int32_t is_last, double arrival_ms);
 
 /* Harvest finished batches and launch the next continuous batch if a chunk
- * is ready and one of the two batch slots is free (never blocks); returns the
- * chunks launched (>= 0) or a status. */
+ * is ready and fewer than serve_batches batches are in flight (never blocks);
+ * returns the chunks launched (>= 0) or a status. */
 int dtwx_serve_step(dtwx_handle *h);
 
 /* Collect decisions made so far (up to cap); returns the count. */
