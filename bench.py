@@ -11,7 +11,10 @@ cells: raw pA samples resident in HBM -> window + z-score kernel -> sDTW sweep
 --impl reference times the CPU implementation of the path (the OpenMP FP64
 restatement of the reference's scripts/sdtw.py `sdtw_default`; the Python
 original needs numba, which is not installed) on a bounded read sample with
-every host thread, and prints the same metric.
+every host thread, and prints the same metric.  Beside it, under
+"reference_gpu_kernel", it times the reference's own FP16 CUDA kernel
+(compiled from its sources into oracle/_ref/) on this GPU, with main.cu's
+10-reads-per-launch pattern and with every read in one launch.
 
 Multi-GPU: reads are independent, each rank runs its own copy of the
 workload (weak scaling, no collective on the data path); the timed region is
@@ -183,6 +186,74 @@ def run_serving(name: str, precision: int, device: int, duration_s: float, batch
     return rec
 
 
+REF_GPU_GEOMETRY = {"C2": "fp16_1000064"}
+
+
+def reference_gpu_kernel(workload, n_reads: int = 2048, shipped_launches: int = 2):
+    """The reference's own FP16 kernel (FullDTW::DTW, src/include/DTW.cu,
+    compiled from its sources into oracle/_ref) on this GPU, on the workload's
+    genome: reads of the kernel's fixed 2,048-sample query from the same
+    generator, levels from the oracle's restatement of the reference's builder.
+    Two launch patterns: main.cu's (BLOCK_NUM = 10 reads per launch, one
+    stream, `shipped_launches` launches timed) and every read in one launch.
+    Returns the record, or {"unavailable": why}."""
+    import torch
+    from dtwax_gb300 import synth
+    from oracle import oracle as O
+    from oracle import ref_kernel as RK
+
+    name = REF_GPU_GEOMETRY.get(workload.name)
+    if name is None:
+        return {"unavailable": f"no reference-kernel geometry for {workload.name} (its query length is fixed "
+                               "at 2,048 samples)"}
+    if not RK.available(name):
+        return {"unavailable": f"{os.path.relpath(RK.cubin_path(name), ROOT)} not built (needs the reference's "
+                               "sources at build time)"}
+    if not torch.cuda.is_available():
+        return {"unavailable": "no CUDA device"}
+    fwd, rev = O.build_levels(workload.genome, workload.table.astype(np.float64))
+    m = fwd.size
+    mask = (np.arange(n_reads) % 2 == 0).astype(np.int8)
+    reads = synth.simulate_reads(workload.genome, workload.other, workload.table, [RK.QUERY_LEN] * n_reads, mask,
+                                 seed=synth.READ_SEED)
+    z = np.stack([O.zscore(reads.read(i).astype(np.float64), 1e-4) for i in range(n_reads)]).astype(np.float32)
+    cells_per_read = float(RK.QUERY_LEN) * m * 2
+    out = {"kernel": "FullDTW::DTW<int, __half2> (src/include/DTW.cu:151-572, -DFP16 -DNO_REF_DEL), "
+                     f"cubin {name}: {m} columns per strand in {-(-m // RK.TILE)} tiles",
+           "query_samples": RK.QUERY_LEN, "unit": "GCUPS"}
+    with RK.RefKernel(name) as k:
+        d_ref = k.reference(fwd.astype(np.float32), rev.astype(np.float32))
+        d_q = k.queries(z)
+        d_dist = torch.empty(n_reads, dtype=torch.int32, device="cuda")
+        d_last = torch.empty(n_reads * k.ref_len, dtype=torch.int32, device="cuda")
+        stream = torch.cuda.current_stream()
+        sh = stream.cuda_stream
+        # warm-up: one small launch
+        k.launch(d_ref, d_q, d_dist, d_last, 2, stream=sh)
+        torch.cuda.synchronize()
+        # main.cu's pattern: 10 reads per launch, launches in sequence
+        b, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        b.record(stream)
+        for i in range(shipped_launches):
+            k.launch(d_ref, d_q, d_dist[i * RK.BLOCK_NUM:], d_last, RK.BLOCK_NUM, first_read=i * RK.BLOCK_NUM,
+                     stream=sh)
+        e.record(stream)
+        torch.cuda.synchronize()
+        ms = b.elapsed_time(e)
+        nr = shipped_launches * RK.BLOCK_NUM
+        out["as_shipped"] = {"value": nr * cells_per_read / (ms * 1e-3) / 1e9, "reads_per_s": nr / (ms * 1e-3),
+                             "ms": ms, "launches": shipped_launches, "reads_per_launch": RK.BLOCK_NUM}
+        # every read in one launch (one warp per read, all resident)
+        b.record(stream)
+        k.launch(d_ref, d_q, d_dist, d_last, n_reads, stream=sh)
+        e.record(stream)
+        torch.cuda.synchronize()
+        ms = b.elapsed_time(e)
+        out["one_launch"] = {"value": n_reads * cells_per_read / (ms * 1e-3) / 1e9,
+                             "reads_per_s": n_reads / (ms * 1e-3), "ms": ms, "reads": n_reads}
+    return out
+
+
 def run_reference(args, rank, world):
     from dtwax_gb300 import synth
     if rank != 0:
@@ -201,6 +272,11 @@ def run_reference(args, rank, world):
             "cpu_baseline": {k: rec[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": rec["value"], "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "reads_per_s": rec["reads_per_s"]}
+    if not args.skip_ref_gpu:
+        try:
+            line["reference_gpu_kernel"] = reference_gpu_kernel(w)
+        except Exception as exc:  # a checker failure must not hide the CPU line
+            line["reference_gpu_kernel"] = {"unavailable": f"{type(exc).__name__}: {exc}"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -352,6 +428,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--skip-ref-gpu", action="store_true",
+                    help="reference arm: do not time the reference's own GPU kernel beside the CPU line")
     ap.add_argument("--precision", choices=["fp16", "fp32"], default="fp16")
     ap.add_argument("--reads", type=int, default=0,
                     help="use only the first N reads of the workload (small cases for profiling)")

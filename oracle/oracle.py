@@ -14,7 +14,8 @@ Two independent restatements of the reference algorithm live here:
 Reference files followed (paths inside harisankarsadasivan/DTWax):
 scripts/sdtw.py:86-116 and :205-225, src/include/DTW.cu:37-39,
 src/include/load_reference.hpp:33-128, src/include/normalizer.cu:397-399,
-src/ReadUntil/calc_classification_threshold.py:49-57.
+src/ReadUntil/calc_classification_threshold.py:49-57, and for the reference
+kernel's own evaluation order src/include/DTW.cu:151-572.
 """
 from __future__ import annotations
 
@@ -60,6 +61,11 @@ def lib():
         L.oracle_sdtw_batch.argtypes = [_d, _d, ctypes.c_int64, _d, _i64, ctypes.c_int,
                                         _d, _i64, _d, _i64, ctypes.c_int]
         L.oracle_sdtw_batch.restype = None
+        L.oracle_sdtw_refkernel.argtypes = [_d, ctypes.c_int64, _d, ctypes.c_int64, ctypes.c_int]
+        L.oracle_sdtw_refkernel.restype = ctypes.c_double
+        L.oracle_sdtw_refkernel_batch.argtypes = [_d, ctypes.c_int64, _d, ctypes.c_int64, ctypes.c_int,
+                                                  ctypes.c_int, _d, ctypes.c_int]
+        L.oracle_sdtw_refkernel_batch.restype = None
         L.oracle_max_threads.argtypes = []
         L.oracle_max_threads.restype = ctypes.c_int
         _lib = L
@@ -147,6 +153,36 @@ def sdtw_batch(fwd, rev, queries, offsets, n_threads: int = 0):
         lib().oracle_sdtw_batch(_dp(fwd), _dp(rev), fwd.size, _dp(queries), _ip(offsets), n,
                                 _dp(sf), _ip(ef), _dp(sr), _ip(er), int(n_threads))
     return sf, ef, sr, er
+
+
+# Departures of the reference GPU kernel from the recurrence (src/include/DTW.cu),
+# switches of oracle_sdtw_refkernel; see sdtw_oracle.c for each.
+REFK_TILE = 832
+REFK_CHUNK = 1024
+REFK_CHUNK_SEAM_DIAG = 1
+REFK_CHUNK_LANE1_DIAG = 2
+REFK_SEAM_SHIFT = 4
+REFK_ALL = 7
+
+
+def sdtw_refkernel(ref, q, quirks: int = REFK_ALL) -> float:
+    """min over the last row in the reference kernel's tile/chunk order with
+    the chosen departures; ref holds whole 832-column tiles, q 1,024-row chunks."""
+    ref = np.ascontiguousarray(ref, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    return float(lib().oracle_sdtw_refkernel(_dp(ref), ref.size, _dp(q), q.size, int(quirks)))
+
+
+def sdtw_refkernel_batch(ref, queries, quirks: int = REFK_ALL, n_threads: int = 0):
+    """sdtw_refkernel for each row of the 2-D array queries (OpenMP)."""
+    ref = np.ascontiguousarray(ref, dtype=np.float64)
+    queries = np.ascontiguousarray(queries, dtype=np.float64)
+    n, qlen = queries.shape
+    out = np.empty(n, np.float64)
+    if n > 0:
+        lib().oracle_sdtw_refkernel_batch(_dp(ref), ref.size, _dp(queries), qlen, n, int(quirks),
+                                          _dp(out), int(n_threads))
+    return out
 
 
 def max_threads() -> int:

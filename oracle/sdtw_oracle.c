@@ -205,6 +205,106 @@ void oracle_sdtw_batch(const double *fwd, const double *rev, int64_t m,
   }
 }
 
+/* The reference GPU kernel's evaluation order, restated in FP64, with its
+ * departures from the recurrence as switches (src/include/DTW.cu:151-572 at
+ * its shipped shape: 832-column tiles of 32 lanes x 26 cells, the query in
+ * 1,024-row chunks, one warp per read).
+ *
+ * The kernel sweeps chunk by chunk and, inside a chunk, tile by tile; a tile
+ * gets the column to its left from the previous tile through a 1,024-entry
+ * seam buffer (DTW.cu:155, :237-262, :369-389) and a chunk gets the row above
+ * it from the previous chunk's last row (DTW.cu:205-209, :325-331, :447-455).
+ * With quirks == 0 this order gives exactly the values of oracle_sdtw.
+ * Switches (OR them):
+ *   REFK_CHUNK_SEAM_DIAG (1): first row of a chunk after the first, first
+ *     column of a tile after the first: diagonal = +inf (the tile starts with
+ *     penalty_diag = inf, DTW.cu:313-315, :441-443);
+ *   REFK_CHUNK_LANE1_DIAG (2): same row, column 26 of every tile (lane 1's
+ *     first cell): diagonal = +inf (lane 1's first update reads the
+ *     penalty_left value set before the wave loop, DTW.cu:178-179, :216-227);
+ *   REFK_SEAM_SHIFT (4): seam rows 961..991 written by a middle tile hold the
+ *     value of the row 31 below (the write index wave - 63 at DTW.cu:387
+ *     against wave - 32 in the first tile, DTW.cu:267), seen by the next tile.
+ * m must be a multiple of 832 with at least two tiles (the kernel's own
+ * geometry, its last partial tile is never scored) and n a multiple of 1024.
+ * Returns min_j D[n-1][j] (the kernel reports no column), or NaN on a bad
+ * shape. */
+#define REFK_TILE 832
+#define REFK_CHUNK 1024
+#define REFK_LANE_CELLS 26
+#define REFK_CHUNK_SEAM_DIAG 1
+#define REFK_CHUNK_LANE1_DIAG 2
+#define REFK_SEAM_SHIFT 4
+
+double oracle_sdtw_refkernel(const double *ref, int64_t m, const double *q, int64_t n, int quirks) {
+  if (m < 2 * REFK_TILE || m % REFK_TILE != 0 || n <= 0 || n % REFK_CHUNK != 0) return NAN;
+  const int64_t tiles = m / REFK_TILE;
+  double *last_in = (double *)calloc((size_t)m, sizeof(double));
+  double *last_out = (double *)malloc(sizeof(double) * (size_t)m);
+  double *seam_prev = (double *)malloc(sizeof(double) * REFK_CHUNK);
+  double *seam_cur = (double *)malloc(sizeof(double) * REFK_CHUNK);
+  double *ra = (double *)malloc(sizeof(double) * REFK_TILE);
+  double *rb = (double *)malloc(sizeof(double) * REFK_TILE);
+  double best = NAN;
+  if (!last_in || !last_out || !seam_prev || !seam_cur || !ra || !rb) goto done;
+  for (int64_t c = 0; c < n / REFK_CHUNK; ++c) {
+    for (int64_t k = 0; k < tiles; ++k) {
+      const int64_t c0 = k * REFK_TILE;
+      const double *up = last_in + c0;
+      double *cur = ra, *spare = rb;
+      for (int64_t r = 0; r < REFK_CHUNK; ++r) {
+        const double qi = q[c * REFK_CHUNK + r];
+        for (int64_t j = 0; j < REFK_TILE; ++j) {
+          const double d = ref[c0 + j] - qi;
+          const double cost = d * d;
+          if (c == 0 && r == 0) {  /* free start */
+            cur[j] = cost;
+            continue;
+          }
+          const double top = up[j];
+          double diag;
+          if (j > 0)
+            diag = up[j - 1];
+          else if (k == 0)
+            diag = INFINITY;
+          else if (r == 0)
+            diag = (quirks & REFK_CHUNK_SEAM_DIAG) ? INFINITY : last_in[c0 - 1];
+          else
+            diag = seam_prev[r - 1];
+          if (r == 0 && j == REFK_LANE_CELLS && (quirks & REFK_CHUNK_LANE1_DIAG)) diag = INFINITY;
+          cur[j] = cost + (top < diag ? top : diag);
+        }
+        seam_cur[r] = cur[REFK_TILE - 1];
+        if (r == REFK_CHUNK - 1) memcpy(last_out + c0, cur, sizeof(double) * REFK_TILE);
+        up = cur;
+        double *sw = cur; cur = spare; spare = sw;
+      }
+      if ((quirks & REFK_SEAM_SHIFT) && k >= 1 && k <= tiles - 2)
+        for (int x = 961; x <= 991; ++x) seam_cur[x] = seam_cur[x + 31];
+      double *sw = seam_prev; seam_prev = seam_cur; seam_cur = sw;
+    }
+    double *sw = last_in; last_in = last_out; last_out = sw;
+  }
+  best = last_in[0];
+  for (int64_t j = 1; j < m; ++j)
+    if (last_in[j] < best) best = last_in[j];
+done:
+  free(last_in); free(last_out); free(seam_prev); free(seam_cur); free(ra); free(rb);
+  return best;
+}
+
+/* oracle_sdtw_refkernel over reads of qlen samples stored back to back,
+ * OpenMP over reads. */
+void oracle_sdtw_refkernel_batch(const double *ref, int64_t m, const double *queries, int64_t qlen,
+                                 int n_reads, int quirks, double *score, int n_threads) {
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int r = 0; r < n_reads; ++r)
+    score[r] = oracle_sdtw_refkernel(ref, m, queries + (int64_t)r * qlen, qlen, quirks);
+}
+
 /* Threads OpenMP will use (reported as the CPU baseline's core count). */
 int oracle_max_threads(void) {
 #ifdef _OPENMP
