@@ -304,7 +304,7 @@ def run_ours(args, rank, world, local):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    precision = d.FP16 if args.precision == "fp16" else d.FP32
+    precision = {"fp16": d.FP16, "fp32": d.FP32, "mixed": d.MIXED}[args.precision]
     w = synth.make_workload(args.workload, n_reads=args.reads or None)
     cells = w.cells()
     n_reads = w.reads.n
@@ -374,17 +374,18 @@ def run_ours(args, rank, world, local):
     achieved = cells / mean_sweep_s / 1e9
     # pipe-bound ceiling from the SM count and the measured SM clock: FP16 cell
     # pairs cost 2 FMA-pipe instructions that hold the pipe 2 cycles each
-    # (64 cells/SM/cycle); FP32 cells cost 3 issue slots (42.7 cells/SM/cycle)
+    # (64 cells/SM/cycle); FP32 cells cost 3 issue slots (42.7 cells/SM/cycle);
+    # MIXED cells cost 2.5 issue slots (half an HSUB2, one FMA, one FMNMX: 51.2)
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     mhz = clock_rec.get("sm_mhz") or 2070.0
-    per_sm_cycle = 64.0 if precision == d.FP16 else 128.0 / 3.0
+    per_sm_cycle = {d.FP16: 64.0, d.FP32: 128.0 / 3.0, d.MIXED: 128.0 / 2.5}[precision]
     theoretical = sms * per_sm_cycle * mhz * 1e6 / 1e9
     traffic = traffic_from_profile(args.precision)
     t_mask = w.reads.target == 1
     line = {
         "metric": "sDTW GCUPS", "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f16x2" if precision == d.FP16 else "f32",
+        "scaling": "weak", "vs_baseline": None, "dtype": {d.FP16: "f16x2", d.FP32: "f32", d.MIXED: "f16-diff/f32"}[precision],
         "data": "synthetic",
         "config": {"workload": f"{args.workload}: {WORKLOAD_DESC[args.workload]}", "cells_per_step": cells,
                    "reads_per_step": n_reads, "ref_columns_per_strand": w.ref_len,
@@ -430,7 +431,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-ref-gpu", action="store_true",
                     help="reference arm: do not time the reference's own GPU kernel beside the CPU line")
-    ap.add_argument("--precision", choices=["fp16", "fp32"], default="fp16")
+    ap.add_argument("--precision", choices=["fp16", "fp32", "mixed"], default="fp16")
     ap.add_argument("--reads", type=int, default=0,
                     help="use only the first N reads of the workload (small cases for profiling)")
     ap.add_argument("--skip-cpu", action="store_true", help="do not time the CPU baseline")

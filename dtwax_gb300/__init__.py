@@ -26,7 +26,7 @@ CLI_PATH = os.path.join(PKG, "bin", "dtwx_main")
 DTWX_OK = 0
 STATUS = {0: "OK", -1: "E_ARG", -2: "E_IO", -3: "E_FORMAT", -4: "E_CUDA", -5: "E_NOMEM",
           -6: "E_TIMEOUT", -7: "E_CAPACITY", -8: "E_STATE"}
-FP16, FP32 = 0, 1
+FP16, FP32, MIXED = 0, 1, 2  # MIXED: FP16 differences, FP32 path cost
 STRANDS_PAIRED, STRANDS_CONCAT = 0, 1
 ABI_VERSION = 1
 

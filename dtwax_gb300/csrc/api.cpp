@@ -31,8 +31,8 @@ namespace {
 
 thread_local std::string g_create_err;
 
-constexpr int64_t kPadCols = 3072;
-constexpr int kServeSlots = 4;      // most serving batches in flight at once, each on its own stream  // a multiple of every compiled strip width (512, 768, 1024, 1536)
+constexpr int64_t kPadCols = 6144;  // a multiple of every compiled strip width (512, 1024, 1536, 2048 columns)
+constexpr int kServeSlots = 4;      // most serving batches in flight at once, each on its own stream
 
 struct Shape {
   int S = 0;      // cells (column pairs) per lane
@@ -85,10 +85,10 @@ struct dtwx_handle {
   int64_t m = 0;       // k-mer positions per strand
   int64_t m_cols = 0;  // DP columns (m, or 2m for the concatenated mode)
   int64_t m_pad = 0;
-  DevBuf ref16, ref32, fwd32, rev32;
-  CUtensorMap tmap[2][3]{};  // [precision][instance index]
-  bool tmap_ok[2][3]{};
-  Shape fixed[2];            // user-fixed parts of the shape (0 = choose)
+  DevBuf ref16, ref32, ref16p, fwd32, rev32;  // FP16 pairs, FP32 planes, FP16 planes (MIXED)
+  CUtensorMap tmap[3][3]{};  // [precision][instance index]
+  bool tmap_ok[3][3]{};
+  Shape fixed[3];            // user-fixed parts of the shape (0 = choose)
   // autotuned shapes by (precision, log2 tasks, log2 rows): S, warps and a
   // factor on the analytic chunk width
   struct Tuned {
@@ -106,7 +106,7 @@ struct dtwx_handle {
   BatchCtx ctx[1 + kServeSlots];  // [0] offline calls, [1..] the serving batches
   std::string err;
   int32_t last_launches = 0;
-  Shape last_shape[2];
+  Shape last_shape[3];
   // serving
   bool serving = false;
   int32_t chunks_per_decision = 3;
@@ -153,7 +153,7 @@ struct CaptureGuard {
   } while (0)
 
 // compiled sweep instances (cells per lane) by precision
-constexpr int kInstS[2][3] = {{32, 48, 0}, {16, 32, 48}};
+constexpr int kInstS[3][3] = {{32, 48, 0}, {16, 32, 48}, {32, 48, 64}};
 int inst_count(int precision) { return precision == 0 ? 2 : 3; }
 int inst_index(int precision, int S) {
   for (int i = 0; i < inst_count(precision); ++i)
@@ -176,17 +176,17 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 // The reference viewed as rows of 128 bytes (32 x u32); one box = one strip
-// (32 lanes x S four-byte elements), loaded with 128-byte swizzling so that
-// each lane's 16-byte reads of its own slice are free of bank conflicts.
-// `elems` = 4-byte elements in the buffer (m_pad pairs for FP16, two planes
-// of m_pad floats for FP32).
-bool make_tmap(CUtensorMap *map, void *base, int64_t elems, int S) {
+// (32 lanes x S columns of ref_bytes each), loaded with 128-byte swizzling so
+// that each lane's 16-byte reads of its own slice are free of bank conflicts.
+// `bytes` = size of the buffer (m_pad FP16 pairs, two planes of m_pad floats,
+// or two planes of m_pad halves).
+bool make_tmap(CUtensorMap *map, void *base, int64_t bytes, int S, int ref_bytes) {
   auto enc = tensor_map_encoder();
   if (!enc) return false;
-  const cuuint64_t rows = (cuuint64_t)(elems * 4 / 128);
+  const cuuint64_t rows = (cuuint64_t)(bytes / 128);
   cuuint64_t dims[2] = {32, rows};
   cuuint64_t strides[1] = {128};
-  cuuint32_t box[2] = {32, (cuuint32_t)(32 * S * 4 / 128)};
+  cuuint32_t box[2] = {32, (cuuint32_t)(32 * S * ref_bytes / 128)};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, base, dims, strides, box, estr,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -217,6 +217,11 @@ int choose_chunk_strips(int64_t strips_per_read, int64_t n_tasks, double mean_ro
     }
   }
   return best_g;
+}
+
+// Reference buffer a sweep of this precision reads when TMA is off.
+const void *ref_for(const dtwx_handle *h, int precision) {
+  return precision == 0 ? h->ref16.p : (precision == 2 ? h->ref16p.p : h->ref32.p);
 }
 
 int log2_bucket(double x) { return x < 1.0 ? 0 : (int)std::floor(std::log2(x)); }
@@ -294,7 +299,7 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
     p.seam = c.seam.as<char>();
     p.counter = counter;
     p.err = err;
-    p.ref_plain = precision == 0 ? h->ref16.p : h->ref32.p;
+    p.ref_plain = ref_for(h, precision);
     p.m = h->m_cols;
     p.m_pad = h->m_pad;
     p.seam_stride = per_warp;
@@ -304,7 +309,7 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
     p.n_chunks = (int32_t)((strips + sh.G - 1) / sh.G);
     p.chunk_strips = sh.G;
     p.max_rows = rows_cap;
-    p.n_items = (int32_t)(n_tasks * p.n_chunks * (precision == 1 ? strands : 1));
+    p.n_items = (int32_t)(n_tasks * p.n_chunks * (precision != 0 ? strands : 1));
     p.ref_layout = 1;
     p.strands = strands;
     const int ii = inst_index(precision, sh.S);
@@ -557,7 +562,7 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
       p.seam = c.seam.as<char>();
       p.counter = counter;
       p.err = counter + 4;
-      p.ref_plain = precision == 0 ? h->ref16.p : h->ref32.p;
+      p.ref_plain = ref_for(h, precision);
       p.m = h->m_cols;
       p.m_pad = h->m_pad;
       p.seam_stride = per_warp;
@@ -568,7 +573,7 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
       p.chunk_strips = sh.G;
       p.max_rows = rows_cap;
       p.strands = h->cfg.strand_mode == DTWX_STRANDS_CONCAT ? 1 : 2;
-      p.n_items = p.n_chunks * (precision == 1 ? p.strands : 1);
+      p.n_items = p.n_chunks * (precision != 0 ? p.strands : 1);
       p.ref_layout = 1;
       const int ii = inst_index(precision, sh.S);
       p.use_tma = h->tmap_ok[precision][ii] ? 1 : 0;
@@ -624,7 +629,8 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
     if (cfg_in->abi_version != DTWX_ABI_VERSION) return fail(nullptr, DTWX_E_ARG, "dtwx_config ABI mismatch");
     cfg = *cfg_in;
   }
-  if (cfg.precision != DTWX_FP16 && cfg.precision != DTWX_FP32) return fail(nullptr, DTWX_E_ARG, "bad precision");
+  if (cfg.precision != DTWX_FP16 && cfg.precision != DTWX_FP32 && cfg.precision != DTWX_MIXED)
+    return fail(nullptr, DTWX_E_ARG, "bad precision");
   if (cfg.strand_mode != DTWX_STRANDS_PAIRED && cfg.strand_mode != DTWX_STRANDS_CONCAT)
     return fail(nullptr, DTWX_E_ARG, "bad strand_mode");
   if (cfg.cells_per_thread && !sdtw_instance_exists(cfg.precision, cfg.cells_per_thread))
@@ -653,7 +659,7 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
   h->m = m;
   h->m_cols = m_cols;
   h->m_pad = (m_cols + kPadCols - 1) / kPadCols * kPadCols;
-  for (int p = 0; p < 2; ++p) {
+  for (int p = 0; p < 3; ++p) {
     h->fixed[p].S = (p == cfg.precision && cfg.cells_per_thread) ? cfg.cells_per_thread : 0;
     h->fixed[p].G = cfg.chunk_strips;
     h->fixed[p].warps = cfg.warps_per_cta;
@@ -673,6 +679,7 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
   cudaStream_t st = h->ctx[0].stream;
   if ((e = h->ref16.ensure(sizeof(__half2) * h->m_pad)) != cudaSuccess) return bad(e, "alloc ref16");
   if ((e = h->ref32.ensure(2 * sizeof(float) * h->m_pad)) != cudaSuccess) return bad(e, "alloc ref32");
+  if ((e = h->ref16p.ensure(2 * sizeof(__half) * h->m_pad)) != cudaSuccess) return bad(e, "alloc ref16p");
   if ((e = h->fwd32.ensure(sizeof(float) * m)) != cudaSuccess) return bad(e, "alloc fwd32");
   if ((e = h->rev32.ensure(sizeof(float) * m)) != cudaSuccess) return bad(e, "alloc rev32");
   DevBuf d_seq, d_table, d_work;
@@ -683,16 +690,19 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
   cudaMemcpyAsync(d_table.p, table.data(), sizeof(double) * kTableSize, cudaMemcpyHostToDevice, st);
   e = launch_build_reference(d_seq.as<char>(), L, d_table.as<double>(), m, h->m_pad,
                              cfg.strand_mode == DTWX_STRANDS_CONCAT, d_work.as<double>(), h->ref16.as<__half2>(),
-                             h->ref32.as<float>(), h->fwd32.as<float>(), h->rev32.as<float>(), st);
+                             h->ref32.as<float>(), h->ref16p.as<__half>(), h->fwd32.as<float>(),
+                             h->rev32.as<float>(), st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   d_seq.release();
   d_table.release();
   d_work.release();
   if (e != cudaSuccess) return bad(e, "reference build");
-  for (int p = 0; p < 2; ++p)
+  for (int p = 0; p < 3; ++p) {
+    const int64_t bytes = p == 0 ? 4 * h->m_pad : (p == 1 ? 8 * h->m_pad : 4 * h->m_pad);
     for (int i = 0; i < inst_count(p); ++i)
-      h->tmap_ok[p][i] = make_tmap(&h->tmap[p][i], p == 0 ? h->ref16.p : h->ref32.p,
-                                   p == 0 ? h->m_pad : 2 * h->m_pad, inst_S(p, i));
+      h->tmap_ok[p][i] = make_tmap(&h->tmap[p][i], const_cast<void *>(ref_for(h, p)), bytes, inst_S(p, i),
+                                   sdtw_ref_bytes(p));
+  }
   *out = h;
   return DTWX_OK;
 }
@@ -985,7 +995,7 @@ int dtwx_get_tuning(const dtwx_handle *h, int32_t *out, int32_t n) {
 }
 
 int dtwx_peak_probe(int32_t device, int32_t precision, float ms_target, double *cells_per_s) {
-  if (!cells_per_s || (precision != 0 && precision != 1)) return DTWX_E_ARG;
+  if (!cells_per_s || precision < 0 || precision > 2) return DTWX_E_ARG;
   if (cudaSetDevice(device) != cudaSuccess) return DTWX_E_CUDA;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);

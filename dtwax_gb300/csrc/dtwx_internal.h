@@ -57,8 +57,9 @@ struct SdtwParams {
   int32_t max_rows;            // capacity of the seam buffers (rows)
   int32_t n_items;             // informational: the kernel derives the queue length itself
   int32_t use_tma;
-  int32_t ref_layout;          // FP32: 0 = interleaved (fwd, rev) float pairs, 1 = planar (rev plane at m_pad)
-  int32_t strands;             // FP32 strands per task: 2 (paired), 1 (concatenated sequence); 0 = 2
+  int32_t ref_layout;          // FP32: 0 = interleaved (fwd, rev) float pairs, 1 = planar (rev plane at m_pad);
+                               // MIXED is always planar FP16
+  int32_t strands;             // FP32/MIXED strands per task: 2 (paired), 1 (concatenated sequence); 0 = 2
 };
 
 // Per-warp scratch layout, in bytes, for cells of `pair_bytes` bytes.
@@ -100,7 +101,7 @@ __host__ __device__ inline float ordered_to_float(uint32_t o) {
 // ---------------------------------------------------------------- launchers
 // (defined in the .cu files; all return cudaError_t of the launch)
 
-// sDTW over all (task, chunk) items.  precision: 0 FP16, 1 FP32.
+// sDTW over all (task, chunk) items.  precision: 0 FP16, 1 FP32, 2 MIXED.
 // cells_per_thread must be one of the compiled instances.
 cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, int grid,
                         const SdtwParams &p, const CUtensorMap *tmap, cudaStream_t s);
@@ -109,13 +110,14 @@ size_t sdtw_smem_bytes(int precision, int cells_per_thread, int warps_per_cta);
 // Resident CTAs per SM for the given shape (occupancy API), 0 on error.
 int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta);
 bool sdtw_instance_exists(int precision, int cells_per_thread);
-int sdtw_pair_bytes(int precision);
+int sdtw_pair_bytes(int precision);  // bytes per DP cell (seam scratch)
+int sdtw_ref_bytes(int precision);   // reference bytes per column of a strip
 
-// Reference builder: genome bytes -> z-scored levels as FP16 (fwd, rev) pairs
-// and as FP32 planes (fwd plane, then rev plane at m_pad).
+// Reference builder: genome bytes -> z-scored levels as FP16 (fwd, rev) pairs,
+// as FP32 planes (fwd plane, then rev plane at m_pad) and as FP16 planes.
 cudaError_t launch_build_reference(const char *d_seq, int64_t L, const double *d_table,
                                    int64_t m, int64_t m_pad, int concat, double *d_work,
-                                   __half2 *d_ref16, float *d_ref32, float *d_fwd32,
+                                   __half2 *d_ref16, float *d_ref32, __half *d_ref16p, float *d_fwd32,
                                    float *d_rev32, cudaStream_t s);
 size_t build_reference_work_bytes(int64_t m);
 

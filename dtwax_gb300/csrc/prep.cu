@@ -148,7 +148,7 @@ __global__ void reduce_sd_kernel(const double *partial, int nblk, double *stats)
 // fwd||rev of 2m columns, stored in both strand slots (the FP32 sweep then
 // aligns only plane 0).
 __global__ void zscore_pairs_kernel(const double *lev, int64_t m, int64_t m_pad, int concat,
-                                    const double *stats, __half2 *ref16, float *ref32,
+                                    const double *stats, __half2 *ref16, float *ref32, __half *ref16p,
                                     float *fwd32, float *rev32) {
   const double mf = stats[0], mr = stats[2];
   const double sf = stats[4] > 0 ? stats[4] : 1.0, sr = stats[5] > 0 ? stats[5] : 1.0;
@@ -173,6 +173,8 @@ __global__ void zscore_pairs_kernel(const double *lev, int64_t m, int64_t m_pad,
     ref32[j] = a;          // fwd plane
     ref32[m_pad + j] = b;  // rev plane
     ref16[j] = __floats2half2_rn(a, b);
+    ref16p[j] = __float2half_rn(a);          // FP16 planes (MIXED precision)
+    ref16p[m_pad + j] = __float2half_rn(b);
   }
 }
 
@@ -183,7 +185,7 @@ size_t build_reference_work_bytes(int64_t m) {
 
 cudaError_t launch_build_reference(const char *d_seq, int64_t L, const double *d_table, int64_t m,
                                    int64_t m_pad, int concat, double *d_work, __half2 *d_ref16,
-                                   float *d_ref32, float *d_fwd32, float *d_rev32,
+                                   float *d_ref32, __half *d_ref16p, float *d_fwd32, float *d_rev32,
                                    cudaStream_t s) {
   const int nblk = 1024;
   double *lev = d_work;
@@ -194,8 +196,8 @@ cudaError_t launch_build_reference(const char *d_seq, int64_t L, const double *d
   reduce_mean_kernel<<<1, kBlock, 0, s>>>(partial, nblk, stats);
   sumsq_kernel<<<nblk, kBlock, 0, s>>>(lev, m, stats, partial, nblk);
   reduce_sd_kernel<<<1, kBlock, 0, s>>>(partial, nblk, stats);
-  zscore_pairs_kernel<<<1024, kBlock, 0, s>>>(lev, m, m_pad, concat, stats, d_ref16, d_ref32, d_fwd32,
-                                              d_rev32);
+  zscore_pairs_kernel<<<1024, kBlock, 0, s>>>(lev, m, m_pad, concat, stats, d_ref16, d_ref32, d_ref16p,
+                                              d_fwd32, d_rev32);
   return cudaGetLastError();
 }
 

@@ -26,6 +26,10 @@
 // an FP32 offset, so the cells near the minimum stay small and precise.  The
 // seam value crossing into the next strip is re-based by the difference of the
 // two strips' offsets (one per epoch of kRescaleRows rows).
+//
+// MIXED: the differences r - q run in FP16 half2 (two adjacent columns of one
+// strand per instruction) and the path cost is FP32: each cell is one
+// mixed-precision FMA d*d + min(...) with f16 d and an f32 addend and result.
 #include "dtwx_internal.h"
 
 #include <cuda/std/cstdint>
@@ -35,16 +39,18 @@ namespace dtwx {
 #define FULL_MASK 0xffffffffu
 
 // ---------------------------------------------------------------- precision policies
-// Both policies keep one 32-bit register per cell so that selects, shuffles
+// Every policy keeps one 32-bit register per cell so that selects, shuffles
 // and seam stores are single instructions.  FP16 packs the two strands of a
 // column into one __half2 (fwd in .x, rev in .y) and a work item covers both;
-// FP32 keeps one strand per cell and a work item covers one strand.
+// FP32 and MIXED keep one strand per cell and a work item covers one strand.
+// RV is the register type of the reference (RB bytes per column).
 
 template <int PREC> struct Pol;
 
 template <> struct Pol<0> {  // FP16 pairs
   using V = __half2;
-  static constexpr int EB = 4;       // bytes per cell / reference element
+  using RV = __half2;
+  static constexpr int RB = 4;       // reference bytes per column
   static constexpr int STRANDS = 1;  // work items per (task, chunk)
   __device__ __forceinline__ static V inf() { return __half2half2(__ushort_as_half((unsigned short)0x7c00u)); }
   __device__ __forceinline__ static V zero() { return __half2half2(__ushort_as_half((unsigned short)0)); }
@@ -70,7 +76,8 @@ template <> struct Pol<0> {  // FP16 pairs
 
 template <> struct Pol<1> {  // FP32, one strand
   using V = float;
-  static constexpr int EB = 4;
+  using RV = float;
+  static constexpr int RB = 4;
   static constexpr int STRANDS = 2;
   __device__ __forceinline__ static V inf() { return __int_as_float(0x7f800000); }
   __device__ __forceinline__ static V zero() { return 0.f; }
@@ -88,6 +95,39 @@ template <> struct Pol<1> {  // FP32, one strand
   __device__ __forceinline__ static QW qw(float q) { return q; }
   __device__ __forceinline__ static V qbcast(QW w, int il) { return __shfl_sync(FULL_MASK, w, il); }
 };
+
+template <> struct Pol<2> {  // MIXED: FP16 differences, FP32 path cost, one strand
+  using V = float;
+  using RV = __half2;                // two adjacent columns of one strand
+  static constexpr int RB = 2;
+  static constexpr int STRANDS = 2;
+  __device__ __forceinline__ static V inf() { return __int_as_float(0x7f800000); }
+  __device__ __forceinline__ static V zero() { return 0.f; }
+  __device__ __forceinline__ static V vmin(V a, V b) { return fminf(a, b); }
+  __device__ __forceinline__ static V shfl(V v, int src) { return __shfl_sync(FULL_MASK, v, src); }
+  __device__ __forceinline__ static V shfl_up(V v) { return __shfl_up_sync(FULL_MASK, v, 1); }
+  __device__ __forceinline__ static V shfl_xor(V v, int m) { return __shfl_xor_sync(FULL_MASK, v, m); }
+  __device__ __forceinline__ static V sel(bool p, V a, V b) { return p ? a : b; }
+  __device__ __forceinline__ static V from_bits(uint32_t u) { return __uint_as_float(u); }
+  using QW = __half2;
+  __device__ __forceinline__ static QW qw(float q) { return __float2half2_rn(q); }
+  __device__ __forceinline__ static QW qbcast(QW w, int il) { return __shfl_sync(FULL_MASK, w, il); }
+};
+
+// d*d + c with d in FP16 and c, the result in FP32, one rounding (PTX
+// fma.rn.f32.f16, sm_100 and later).
+__device__ __forceinline__ float fma_sq_f16(__half d, float c) {
+  float r;
+  asm("fma.rn.f32.f16 %0, %1, %1, %2;" : "=f"(r) : "h"(__half_as_ushort(d)), "f"(c));
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ T bits_as(uint32_t u) {
+  T v;
+  memcpy(&v, &u, 4);
+  return v;
+}
 
 // ---------------------------------------------------------------- TMA / mbarrier helpers
 
@@ -190,35 +230,35 @@ __device__ __forceinline__ uint32_t swz128(uint32_t b) {
 }
 
 // ---------------------------------------------------------------- ref strip -> registers
-// Lane l's slice of a strip: S consecutive 4-byte elements at byte (l*S)*4.
+// Lane l's slice of a strip: NW consecutive 32-bit words at byte (l*NW)*4
+// (S columns: NW = S for 4-byte columns, S/2 for FP16 columns of one strand).
 
-template <int S, int PREC>
-__device__ __forceinline__ void regs_from_smem(const unsigned char *tile, int lane,
-                                               typename Pol<PREC>::V (&R)[S]) {
-  static_assert((S * 4) % 16 == 0, "lane slice must be 16-byte aligned");
+template <int NW, typename RV>
+__device__ __forceinline__ void regs_from_smem(const unsigned char *tile, int lane, RV (&R)[NW]) {
+  static_assert((NW * 4) % 16 == 0, "lane slice must be 16-byte aligned");
 #pragma unroll
-  for (int k = 0; k < S; k += 4) {
-    const uint32_t b = (uint32_t)((lane * S + k) * 4);
+  for (int k = 0; k < NW; k += 4) {
+    const uint32_t b = (uint32_t)((lane * NW + k) * 4);
     const uint4 v = *reinterpret_cast<const uint4 *>(tile + swz128(b));
-    R[k] = Pol<PREC>::from_bits(v.x);
-    R[k + 1] = Pol<PREC>::from_bits(v.y);
-    R[k + 2] = Pol<PREC>::from_bits(v.z);
-    R[k + 3] = Pol<PREC>::from_bits(v.w);
+    R[k] = bits_as<RV>(v.x);
+    R[k + 1] = bits_as<RV>(v.y);
+    R[k + 2] = bits_as<RV>(v.z);
+    R[k + 3] = bits_as<RV>(v.w);
   }
 }
 
-// Contiguous elements from global memory (FP16 pairs, or one FP32 strand plane).
-template <int S, int PREC>
-__device__ __forceinline__ void regs_from_global(const void *base_elem, int lane,
-                                                 typename Pol<PREC>::V (&R)[S]) {
-  const uint4 *g = reinterpret_cast<const uint4 *>(reinterpret_cast<const uint32_t *>(base_elem) + lane * S);
+// Contiguous words from global memory (FP16 pairs, one FP32 strand plane, or
+// one FP16 strand plane).
+template <int NW, typename RV>
+__device__ __forceinline__ void regs_from_global(const void *base, int lane, RV (&R)[NW]) {
+  const uint4 *g = reinterpret_cast<const uint4 *>(reinterpret_cast<const uint32_t *>(base) + lane * NW);
 #pragma unroll
-  for (int k = 0; k < S; k += 4) {
+  for (int k = 0; k < NW; k += 4) {
     const uint4 v = __ldg(g + k / 4);
-    R[k] = Pol<PREC>::from_bits(v.x);
-    R[k + 1] = Pol<PREC>::from_bits(v.y);
-    R[k + 2] = Pol<PREC>::from_bits(v.z);
-    R[k + 3] = Pol<PREC>::from_bits(v.w);
+    R[k] = bits_as<RV>(v.x);
+    R[k + 1] = bits_as<RV>(v.y);
+    R[k + 2] = bits_as<RV>(v.z);
+    R[k + 3] = bits_as<RV>(v.w);
   }
 }
 
@@ -268,6 +308,21 @@ __device__ __forceinline__ void sweep_row(typename Pol<PREC>::V (&D)[S], const t
   D[0] = P::cell(R[0], qq, D[0], left);
 }
 
+// The MIXED row: reference columns 2k and 2k+1 of the lane share one half2,
+// so one HSUB2 gives both differences; each cell is one FP32-result FMA.
+template <int S>
+__device__ __forceinline__ void sweep_row_mixed(float (&D)[S], const __half2 (&R)[S / 2], __half2 qq, float seam,
+                                                uint32_t m0) {
+  const float up = __shfl_up_sync(FULL_MASK, D[S - 1], 1);
+  const float left = __uint_as_float((__float_as_uint(up) & ~m0) | (__float_as_uint(seam) & m0));
+#pragma unroll
+  for (int k = S / 2 - 1; k >= 0; --k) {
+    const __half2 d = __hsub2(R[k], qq);
+    D[2 * k + 1] = fma_sq_f16(__high2half(d), fminf(D[2 * k + 1], D[2 * k]));
+    D[2 * k] = fma_sq_f16(__low2half(d), fminf(D[2 * k], k > 0 ? D[2 * k - 1] : left));
+  }
+}
+
 // Warp-wide lexicographic min of (value, column).
 __device__ __forceinline__ void warp_argmin(float &v, int64_t &j) {
 #pragma unroll
@@ -289,20 +344,35 @@ __device__ __forceinline__ unsigned long long make_key(float v, int64_t j) {
 
 // Register cap per instance: the S cells and S reference elements of a lane
 // plus about 40 registers of bookkeeping, rounded to 128 or 168 (16 or 12 warps/SM).
+// One DP row for the policy: FP16 pairs and FP32 share sweep_row, MIXED has its own.
 template <int S, int PREC>
-constexpr int sdtw_reg_cap() { return 2 * S + 40 <= 128 ? 128 : 168; }
+__device__ __forceinline__ void row(typename Pol<PREC>::V (&D)[S],
+                                    const typename Pol<PREC>::RV (&R)[S * Pol<PREC>::RB / 4],
+                                    typename Pol<PREC>::QW qq, typename Pol<PREC>::V seam, uint32_t m0) {
+  if constexpr (PREC == 2)
+    sweep_row_mixed<S>(D, R, qq, seam, m0);
+  else
+    sweep_row<S, PREC>(D, R, qq, seam, m0);
+}
+
+template <int S, int PREC>
+constexpr int sdtw_reg_cap() { return S + S * Pol<PREC>::RB / 4 + 40 <= 128 ? 128 : 168; }
 
 template <int S, int PREC>
 __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_constant__ CUtensorMap tmap,
                                                                     const SdtwParams p) {
   using P = Pol<PREC>;
   using V = typename P::V;
+  using RV = typename P::RV;
+  constexpr bool PAIRS = PREC == 0;           // both strands in one cell (FP16)
   constexpr int W = kWarp * S;                // columns per strip
-  constexpr int EB = P::EB;
-  constexpr int STRIP_BYTES = W * EB;
+  constexpr int RB = P::RB;                   // reference bytes per column
+  constexpr int NW = S * RB / 4;              // reference words per lane
+  constexpr int CB = 4;                       // bytes per cell
+  constexpr int STRIP_BYTES = W * RB;
   constexpr int K = kRescaleRows;
   static_assert(STRIP_BYTES % 1024 == 0, "strip tile must keep 1024-byte alignment");
-  static_assert(S % 4 == 0, "row state and reference move in 16-byte groups");
+  static_assert(S % 8 == 0, "row state and reference move in 16-byte groups");
 
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
@@ -326,10 +396,10 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
   const int64_t gwarp = (int64_t)blockIdx.x * nwarps + warp;
   char *seam_base = p.seam + gwarp * p.seam_stride;
   const int64_t seam_half = p.seam_stride / 2;
-  const int64_t off_pos = seam_offsets_pos(EB, p.max_rows);
+  const int64_t off_pos = seam_offsets_pos(CB, p.max_rows);
   const int64_t C = (int64_t)p.chunk_strips * W;
-  // FP32 splits each (task, chunk) into one work item per strand
-  const int nstr = PREC == 1 ? (p.strands > 0 ? p.strands : 2) : 1;
+  // FP32 and MIXED split each (task, chunk) into one work item per strand
+  const int nstr = !PAIRS ? (p.strands > 0 ? p.strands : 2) : 1;
   const int per_task = p.n_chunks * nstr;
   const int64_t n_items = (int64_t)p.n_tasks * per_task;
 
@@ -338,7 +408,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
     if (item >= n_items) break;
     const int tr = item / per_task;
     const int rem = item - tr * per_task;
-    const int strand = PREC == 1 ? rem / p.n_chunks : 0;
+    const int strand = !PAIRS ? rem / p.n_chunks : 0;
     const int chunk = rem - strand * p.n_chunks;
     const int ti = p.order ? p.order[tr] : tr;
     const Task t = p.tasks[ti];
@@ -360,15 +430,15 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
     const bool save = (t.flags & kTaskSaveState) != 0 && p.state != nullptr;
     // planar row state: strand s of this read at state + state_off + s*m_pad
     const float *st_plane0 = p.state ? p.state + t.state_off : nullptr;
-    // element offset of this item's strand in a planar FP32 reference
-    const int64_t ref_plane = PREC == 1 && p.ref_layout == 1 ? (int64_t)strand * p.m_pad : 0;
+    // column offset of this item's strand in a planar reference (FP32 planes, or MIXED FP16 planes)
+    const int64_t ref_plane = (PREC == 2 || (PREC == 1 && p.ref_layout == 1)) ? (int64_t)strand * p.m_pad : 0;
 
     float bestx = __int_as_float(0x7f800000), besty = bestx;
     int64_t colx = -1, coly = -1;
 
     if (p.use_tma) {
       fence_proxy_async_smem();
-      tma_issue_if(slot0, &tmap, &bars[0], 0, (int)((ref_plane + x0) * EB / 128), STRIP_BYTES, is0);
+      tma_issue_if(slot0, &tmap, &bars[0], 0, (int)((ref_plane + x0) * RB / 128), STRIP_BYTES, is0);
     }
 
     for (int s = 0; s < nstrips; ++s) {
@@ -436,7 +506,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
       }
 
       // -- reference strip into registers (after the row state: fewer live registers)
-      V R[S];
+      RV R[NW];
       if (p.use_tma) {
         const int sl = s & 1;
         // every lane waits (acquire of the TMA bytes); the give-up decision is warp-uniform
@@ -446,21 +516,23 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
           return;
         }
         phase ^= 1u << sl;
-        regs_from_smem<S, PREC>(slot0 + sl * STRIP_BYTES, lane, R);
+        regs_from_smem<NW, RV>(slot0 + sl * STRIP_BYTES, lane, R);
         __syncwarp();
         if (s + 1 < nstrips) {
           const int ns = (s + 1) & 1;
           fence_proxy_async_smem();
-          tma_issue_if(slot0 + ns * STRIP_BYTES, &tmap, &bars[ns], 0, (int)((ref_plane + x + W) * EB / 128),
+          tma_issue_if(slot0 + ns * STRIP_BYTES, &tmap, &bars[ns], 0, (int)((ref_plane + x + W) * RB / 128),
                        STRIP_BYTES, is0);
         }
       } else if constexpr (PREC == 1) {
         if (p.ref_layout == 0)
           regs_from_pairs<S>(reinterpret_cast<const float2 *>(p.ref_plain), x, lane, strand, R);
         else
-          regs_from_global<S, PREC>(reinterpret_cast<const float *>(p.ref_plain) + ref_plane + x, lane, R);
+          regs_from_global<NW, RV>(reinterpret_cast<const float *>(p.ref_plain) + ref_plane + x, lane, R);
+      } else if constexpr (PREC == 2) {
+        regs_from_global<NW, RV>(reinterpret_cast<const __half *>(p.ref_plain) + ref_plane + x, lane, R);
       } else {
-        regs_from_global<S, PREC>(reinterpret_cast<const __half2 *>(p.ref_plain) + x, lane, R);
+        regs_from_global<NW, RV>(reinterpret_cast<const __half2 *>(p.ref_plain) + x, lane, R);
       }
 
       // uniform stores (every lane writes the same value): no lane-dependent branch
@@ -497,7 +569,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
         if (rows - i0 >= kWarp) {
 #pragma unroll 4
           for (int il = 0; il < kWarp; ++il) {
-            sweep_row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+            row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
             sout = P::sel(lane == il, P::shfl(D[S - 1], 31), sout);
           }
           if constexpr (PREC == 0) {
@@ -524,7 +596,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
         } else {
           const int cnt = rows - i0;
           for (int il = 0; il < cnt; ++il) {
-            sweep_row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+            row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
             sout = P::sel(lane == il, P::shfl(D[S - 1], 31), sout);
           }
           so[lane] = sout;  // lanes >= cnt write +inf into the buffer's 32-entry slack past the rows
@@ -628,13 +700,16 @@ static int occ_inst(int warps) {
 
 int sdtw_pair_bytes(int precision) { (void)precision; return 4; }
 
+int sdtw_ref_bytes(int precision) { return precision == 2 ? 2 : 4; }
+
 size_t sdtw_smem_bytes(int precision, int cells_per_thread, int warps_per_cta) {
-  const size_t strip = (size_t)kWarp * cells_per_thread * sdtw_pair_bytes(precision);
+  const size_t strip = (size_t)kWarp * cells_per_thread * sdtw_ref_bytes(precision);
   return 1024 /* alignment slack */ + 2 * warps_per_cta * strip + 16 * warps_per_cta;
 }
 
 bool sdtw_instance_exists(int precision, int S) {
   if (precision == 0) return S == 32 || S == 48;
+  if (precision == 2) return S == 32 || S == 48 || S == 64;
   return S == 16 || S == 32 || S == 48;
 }
 
@@ -648,6 +723,9 @@ cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, 
   DTWX_DISPATCH(1, 16, launch_inst)(warps_per_cta, grid, p, tmap, s);
   DTWX_DISPATCH(1, 32, launch_inst)(warps_per_cta, grid, p, tmap, s);
   DTWX_DISPATCH(1, 48, launch_inst)(warps_per_cta, grid, p, tmap, s);
+  DTWX_DISPATCH(2, 32, launch_inst)(warps_per_cta, grid, p, tmap, s);
+  DTWX_DISPATCH(2, 48, launch_inst)(warps_per_cta, grid, p, tmap, s);
+  DTWX_DISPATCH(2, 64, launch_inst)(warps_per_cta, grid, p, tmap, s);
   return cudaErrorInvalidValue;
 }
 
@@ -657,6 +735,9 @@ int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta) {
   DTWX_DISPATCH(1, 16, occ_inst)(warps_per_cta);
   DTWX_DISPATCH(1, 32, occ_inst)(warps_per_cta);
   DTWX_DISPATCH(1, 48, occ_inst)(warps_per_cta);
+  DTWX_DISPATCH(2, 32, occ_inst)(warps_per_cta);
+  DTWX_DISPATCH(2, 48, occ_inst)(warps_per_cta);
+  DTWX_DISPATCH(2, 64, occ_inst)(warps_per_cta);
   return 0;
 }
 
@@ -671,6 +752,33 @@ __device__ __forceinline__ typename Pol<PREC>::V probe_value(float a, float b) {
     return __floats2half2_rn(a, b);
   else
     return a;
+}
+
+// MIXED: the same row with half2 reference pairs and FP32 cells.
+__global__ void __launch_bounds__(256) peak_probe_mixed_kernel(int iters, float *sink) {
+  constexpr int S = 32;
+  __half2 R[S / 2];
+  float D[S];
+  const float t = (float)(threadIdx.x & 7) * 0.01f;
+#pragma unroll
+  for (int k = 0; k < S / 2; ++k) R[k] = __floats2half2_rn(t + 0.06f * k, t - 0.042f * k);
+#pragma unroll
+  for (int k = 0; k < S; ++k) D[k] = 0.f;
+  float qf = 0.25f + t;
+  for (int it = 0; it < iters; ++it) {
+    const __half2 qq = __float2half2_rn(qf);
+#pragma unroll
+    for (int k = S / 2 - 1; k >= 0; --k) {
+      const __half2 d = __hsub2(R[k], qq);
+      D[2 * k + 1] = fma_sq_f16(__high2half(d), fminf(D[2 * k + 1], D[2 * k]));
+      D[2 * k] = fma_sq_f16(__low2half(d), fminf(D[2 * k], k > 0 ? D[2 * k - 1] : D[S - 1]));
+    }
+    qf = fmaf(qf, 0.999f, 0.0137f);
+  }
+  float acc = D[0];
+#pragma unroll
+  for (int k = 1; k < S; ++k) acc = fminf(acc, D[k]);
+  if (acc == 12345.678f) sink[threadIdx.x] = acc;
 }
 
 template <int PREC>
@@ -709,6 +817,8 @@ cudaError_t launch_peak_probe(int precision, int grid, int block, int iters, flo
                               cudaStream_t s) {
   if (precision == 0)
     peak_probe_kernel<0><<<grid, block, 0, s>>>(iters, sink);
+  else if (precision == 2)
+    peak_probe_mixed_kernel<<<grid, block, 0, s>>>(iters, sink);
   else
     peak_probe_kernel<1><<<grid, block, 0, s>>>(iters, sink);
   return cudaGetLastError();

@@ -39,8 +39,10 @@ extern "C" {
 #define DTWX_E_STATE (-8)    /* call not valid in the handle's current state */
 
 /* arithmetic of the DP */
-#define DTWX_FP16 0 /* half2 (fwd, rev) cells, per-strip running-min offset kept in FP32 */
-#define DTWX_FP32 1 /* float2 (fwd, rev) cells */
+#define DTWX_FP16 0  /* half2 (fwd, rev) cells, per-strip running-min offset kept in FP32 */
+#define DTWX_FP32 1  /* float cells, one strand per work item */
+#define DTWX_MIXED 2 /* FP16 differences (half2: two columns of one strand), FP32 cells:
+                        each cell is one f32 = f16*f16 + f32 FMA */
 
 /* how the two strands are scored */
 #define DTWX_STRANDS_PAIRED 0 /* fwd and rev aligned separately (DTW.cu half2 .x/.y) */
@@ -48,7 +50,7 @@ extern "C" {
 
 typedef struct dtwx_config {
   int32_t abi_version;     /* DTWX_ABI_VERSION */
-  int32_t precision;       /* DTWX_FP16 (default) or DTWX_FP32 */
+  int32_t precision;       /* DTWX_FP16 (default), DTWX_FP32 or DTWX_MIXED */
   int32_t strand_mode;     /* DTWX_STRANDS_PAIRED (default) or DTWX_STRANDS_CONCAT */
   int32_t device;          /* CUDA device ordinal */
   int64_t max_ref_len;     /* cap on k-mer positions per strand, 0 = none

@@ -18,6 +18,7 @@ pytestmark = pytest.mark.gpu
 
 FP32_RTOL = 1e-5
 FP16_RTOL = 1e-2
+MIXED_RTOL = 1e-3  # FP16 differences, FP32 path cost
 
 
 @pytest.fixture(scope="module")
@@ -66,7 +67,7 @@ def test_reference_builder_nonacgt_and_cap(lib, oracle):
     np.testing.assert_allclose(rev, orv, atol=2e-6)
 
 
-@pytest.mark.parametrize("precision,rtol", [(1, 1e-5), (0, 1e-2)])
+@pytest.mark.parametrize("precision,rtol", [(1, FP32_RTOL), (0, FP16_RTOL), (2, MIXED_RTOL)])
 def test_kat_lambda_on_gpu(lib, kat, tmp_path, precision, rtol):
     """scripts/log on the GPU: the 4096 golden query samples against the
     lambda fwd||rev reference cut to 48,128 k-mers per strand."""
@@ -85,7 +86,7 @@ def test_kat_lambda_on_gpu(lib, kat, tmp_path, precision, rtol):
         assert res["end_pos"][0] == 33305 and res["strand"][0] == 0
 
 
-@pytest.mark.parametrize("precision", [1, 0])
+@pytest.mark.parametrize("precision", [1, 0, 2])
 def test_classify_matches_oracle(lib, oracle, genome_pair, precision):
     g, o = genome_pair
     tab = synth.level_table()
@@ -99,8 +100,9 @@ def test_classify_matches_oracle(lib, oracle, genome_pair, precision):
         check_fp32(res, ora)
     else:
         sf, ef, sr, er = ora
-        np.testing.assert_allclose(res["score_fwd"], sf, rtol=FP16_RTOL, atol=1e-2)
-        np.testing.assert_allclose(res["score_rev"], sr, rtol=FP16_RTOL, atol=1e-2)
+        rtol = FP16_RTOL if precision == 0 else MIXED_RTOL
+        np.testing.assert_allclose(res["score_fwd"], sf, rtol=rtol, atol=1e-2)
+        np.testing.assert_allclose(res["score_rev"], sr, rtol=rtol, atol=1e-2)
         # targets (even indices, >= 500 samples) must end where the oracle ends
         for i, n in enumerate(lengths):
             if i % 2 == 0 and n >= 500:
@@ -122,6 +124,25 @@ def test_fp32_chunking_is_exact(lib, genome_pair, cells, strips, warps):
         t = clf.tuning()
     strips_per_read = -(-(len(g) - 5) // (32 * cells))
     assert t["cells_per_thread"] == cells and t["chunk_strips"] == min(strips, strips_per_read)
+    np.testing.assert_array_equal(res["score_fwd"], base["score_fwd"])
+    np.testing.assert_array_equal(res["score_rev"], base["score_rev"])
+    np.testing.assert_array_equal(res["end_pos"], base["end_pos"])
+
+
+@pytest.mark.parametrize("cells,strips,warps", [(32, 1, 8), (48, 3, 2), (64, 2, 4), (32, 50, 1)])
+def test_mixed_chunking_is_exact(lib, genome_pair, cells, strips, warps):
+    """MIXED keeps FP32 cells with no rescale: any chunk size gives the same bits."""
+    import dtwax_gb300 as d
+    g, o = genome_pair
+    tab = synth.level_table()
+    reads = reads_of_lengths(g, o, tab, [1500, 2000, 700, 2500, 90])
+    with make_classifier(g, tab, precision=d.MIXED) as clf:
+        base = clf.classify(raw=reads.raw, offsets=reads.offsets)
+    with make_classifier(g, tab, precision=d.MIXED, cells_per_thread=cells, chunk_strips=strips,
+                         warps_per_cta=warps) as clf:
+        res = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        t = clf.tuning()
+    assert t["cells_per_thread"] == cells
     np.testing.assert_array_equal(res["score_fwd"], base["score_fwd"])
     np.testing.assert_array_equal(res["score_rev"], base["score_rev"])
     np.testing.assert_array_equal(res["end_pos"], base["end_pos"])
@@ -226,26 +247,35 @@ def test_targets_found_at_true_position(lib):
     assert res["score"][t].max() < res["score"][~t].min()
 
 
-def test_c1_full_parity_fp32_and_fp16(lib, oracle):
-    """All 512 reads of the C1 workload against the FP64 oracle."""
+def test_c1_full_parity_all_precisions(lib, oracle):
+    """All 512 reads of the C1 workload against the FP64 oracle, in FP32,
+    FP16 and MIXED."""
+    import dtwax_gb300 as d
     w = synth.make_workload("C1")
     with make_classifier(w.genome, w.table, precision=1) as clf:
         r32 = clf.classify(raw=w.reads.raw, offsets=w.reads.offsets)
         ora = oracle_classify(oracle, clf, w.reads.raw, w.reads.offsets)
     with make_classifier(w.genome, w.table, precision=0) as clf:
         r16 = clf.classify(raw=w.reads.raw, offsets=w.reads.offsets)
+    with make_classifier(w.genome, w.table, precision=d.MIXED) as clf:
+        rmx = clf.classify(raw=w.reads.raw, offsets=w.reads.offsets)
     sf, ef, sr, er = ora
     np.testing.assert_allclose(r32["score_fwd"], sf, rtol=FP32_RTOL)
     np.testing.assert_allclose(r32["score_rev"], sr, rtol=FP32_RTOL)
     best = np.minimum(sf, sr)
     np.testing.assert_allclose(r16["score"], best, rtol=FP16_RTOL)
+    np.testing.assert_allclose(rmx["score_fwd"], sf, rtol=MIXED_RTOL)
+    np.testing.assert_allclose(rmx["score_rev"], sr, rtol=MIXED_RTOL)
     score, end, strand = oracle.combine(sf, ef, sr, er)
     assert (r32["end_pos"] == end).mean() >= 0.999
+    t = w.reads.target == 1
+    assert ((np.abs(rmx["end_pos"] - end) <= 2) & (rmx["strand"] == strand))[t].mean() >= 0.999
     # classification agreement at the oracle-tuned threshold
     from dtwax_gb300 import threshold
-    th, acc = threshold.best_threshold(best[w.reads.target == 1], best[w.reads.target == 0])
-    agree = (threshold.call(r16["score"], th) == threshold.call(best, th)).mean()
-    assert agree >= 0.999
+    th, acc = threshold.best_threshold(best[t], best[~t])
+    for r in (r16, rmx):
+        agree = (threshold.call(r["score"], th) == threshold.call(best, th)).mean()
+        assert agree >= 0.999
 
 
 def test_cli_drop_in(lib, kat, tmp_path):
