@@ -28,7 +28,7 @@ STATUS = {0: "OK", -1: "E_ARG", -2: "E_IO", -3: "E_FORMAT", -4: "E_CUDA", -5: "E
           -6: "E_TIMEOUT", -7: "E_CAPACITY", -8: "E_STATE"}
 FP16, FP32, MIXED = 0, 1, 2  # MIXED: FP16 differences, FP32 path cost
 STRANDS_PAIRED, STRANDS_CONCAT = 0, 1
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 
 class DtwxError(RuntimeError):
@@ -60,7 +60,7 @@ class Decision(ctypes.Structure):
     _fields_ = [("channel", ctypes.c_int32), ("decided", ctypes.c_int32), ("read_number", ctypes.c_uint64),
                 ("score", ctypes.c_float), ("strand", ctypes.c_int32), ("call", ctypes.c_int32),
                 ("end_pos", ctypes.c_int64), ("chunks", ctypes.c_int32), ("samples", ctypes.c_int32),
-                ("latency_ms", ctypes.c_double)]
+                ("latency_ms", ctypes.c_double), ("queue_ms", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -70,7 +70,8 @@ class Stats(ctypes.Structure):
                 ("max_in_flight", ctypes.c_int32), ("batches", ctypes.c_int32),
                 ("p50_latency_ms", ctypes.c_double), ("p99_latency_ms", ctypes.c_double),
                 ("mean_batch_reads", ctypes.c_double), ("state_bytes", ctypes.c_double),
-                ("mean_batch_ms", ctypes.c_double), ("max_batch_ms", ctypes.c_double)]
+                ("mean_batch_ms", ctypes.c_double), ("max_batch_ms", ctypes.c_double),
+                ("p50_queue_ms", ctypes.c_double), ("p99_queue_ms", ctypes.c_double)]
 
 
 # numpy view of dtwx_result (32 bytes)

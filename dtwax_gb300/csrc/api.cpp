@@ -74,6 +74,7 @@ struct ServeTask {
   int n;
   double arrival;
   int last;
+  double launched = 0;  // host time the batch holding this chunk was launched
 };
 
 }  // namespace
@@ -117,7 +118,7 @@ struct dtwx_handle {
   std::map<std::pair<int32_t, uint64_t>, double> finished;  // decided reads -> decision time
   std::deque<std::pair<int32_t, uint64_t>> admit_queue;
   std::vector<dtwx_decision> decisions;
-  std::vector<double> latencies;
+  std::vector<double> latencies, queue_times;  // decided reads
   std::vector<ServeTask> inflight[kServeSlots];  // tasks of the serving batch in ctx[1 + s]
   bool running[kServeSlots] = {};
   float accept_per_sample = 0.f, reject_per_sample = 0.f;
@@ -236,8 +237,11 @@ Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_row
   double g_scale = 1.0;
   auto t = h->tuned.find(std::make_tuple(precision, log2_bucket((double)n_tasks), log2_bucket(mean_rows)));
   const bool use_t = t != h->tuned.end();
-  s.S = o.S ? o.S : (f.S ? f.S : (use_t ? t->second.S : 32));
-  s.warps = o.warps ? o.warps : (f.warps ? f.warps : (use_t ? t->second.warps : 8));
+  // defaults measured on the 1 Mb / 2,048-read batch: 48 cells per lane (64 for
+  // MIXED, whose reference takes half the registers) in 4-warp CTAs
+  const int def_S = precision == 2 ? 64 : 48;
+  s.S = o.S ? o.S : (f.S ? f.S : (use_t ? t->second.S : def_S));
+  s.warps = o.warps ? o.warps : (f.warps ? f.warps : (use_t ? t->second.warps : 4));
   if (use_t && !f.G) g_scale = t->second.g_scale;
   if (o.S) g_scale = o.items > 0 ? o.items / 1000.0 : 1.0;  // candidate factor (per mille) while tuning
   int occ = sdtw_ctas_per_sm(precision, s.S, s.warps);
@@ -919,10 +923,13 @@ int dtwx_autotune(dtwx_handle *h, int32_t n_reads_req, int32_t read_len, float *
   if (!h || n_reads_req <= 0 || read_len <= 0) return DTWX_E_ARG;
   CK(h, cudaSetDevice(h->device));
   const int prec = h->cfg.precision;
-  // candidates are timed on at most 1024 reads; the winner is kept for the
-  // requested batch size (its chunk width is a factor on the analytic model,
-  // which rescales with the batch)
-  const int32_t n_reads = std::min<int32_t>(n_reads_req, 1024);
+  // candidates are timed on the requested batch, cut to about 1.2e13 cells
+  // (under a second per candidate) and to 2,048 reads; the winner is kept for
+  // the requested batch size (its chunk width is a factor on the analytic
+  // model, which rescales with the batch)
+  const double per_read = 2.0 * (double)read_len * (double)h->m;
+  const int32_t by_cells = (int32_t)std::max(16.0, std::min(2048.0, 1.2e13 / std::max(per_read, 1.0)));
+  const int32_t n_reads = std::min<int32_t>(n_reads_req, by_cells);
   // synthetic z-scored reads of the requested shape (the sweep's cost does not
   // depend on the sample values)
   std::vector<float> q((size_t)n_reads * read_len);
@@ -950,7 +957,10 @@ int dtwx_autotune(dtwx_handle *h, int32_t n_reads_req, int32_t read_len, float *
   float best = 1e30f;
   Cand win{0, 0, 1000};
   int rc = DTWX_OK;
+  // one untimed pass first: the first sweep of a handle pays one-time costs
+  rc = dtwx_distances(h, dq.as<float>(), offs.data(), n_reads, dout.as<dtwx_result>(), st);
   for (const Cand &cd : cands) {
+    if (rc != DTWX_OK) break;
     h->override_shape = Shape{};
     h->override_shape.S = cd.S;
     h->override_shape.warps = cd.warps;
@@ -1175,6 +1185,7 @@ int harvest(dtwx_handle *h, int slot) {
     d.chunks = r.chunks_done;
     d.samples = r.samples_done;
     d.latency_ms = t - st.arrival;
+    d.queue_ms = st.launched - st.arrival;
     const double per = (double)res[i].score / std::max(r.samples_done, 1);
     const bool target = h->accept_per_sample > 0 ? per < h->accept_per_sample : res[i].score < h->cfg.threshold;
     const bool reject = h->reject_per_sample > 0 && per > h->reject_per_sample;
@@ -1183,6 +1194,7 @@ int harvest(dtwx_handle *h, int slot) {
     h->decisions.push_back(d);
     if (d.decided) {
       h->latencies.push_back(d.latency_ms);
+      h->queue_times.push_back(d.queue_ms);
       ++h->reads_decided;
       release_read(h, it);
     }
@@ -1299,6 +1311,8 @@ int dtwx_serve_step(dtwx_handle *h) {
   CK(h, c.h_flags.ensure(64));
   CK(h, cudaMemcpyAsync(c.h_flags.p, c.flags.p, 64, cudaMemcpyDeviceToHost, st));  // read at harvest
   CK(h, cudaEventRecord(c.done, st));
+  const double launched = now_ms();
+  for (ServeTask &t : batch) t.launched = launched;
   h->inflight[slot] = batch;
   h->running[slot] = true;
   h->batches += 1;
@@ -1347,18 +1361,18 @@ int dtwx_stats_get(dtwx_handle *h, dtwx_stats *out) {
   out->mean_batch_ms = h->batches ? h->batch_ms_sum / h->batches : 0.0;
   out->max_batch_ms = h->batch_ms_max;
   out->state_bytes = (double)h->state.cap;
-  if (!h->latencies.empty()) {
-    std::vector<double> v = h->latencies;
+  auto pct = [](std::vector<double> v, double p) {
+    if (v.empty()) return 0.0;
     std::sort(v.begin(), v.end());
-    auto pct = [&](double p) {
-      const double pos = p * (double)(v.size() - 1);
-      const size_t lo = (size_t)pos;
-      const size_t hi = std::min(lo + 1, v.size() - 1);
-      return v[lo] + (v[hi] - v[lo]) * (pos - (double)lo);
-    };
-    out->p50_latency_ms = pct(0.50);
-    out->p99_latency_ms = pct(0.99);
-  }
+    const double pos = p * (double)(v.size() - 1);
+    const size_t lo = (size_t)pos;
+    const size_t hi = std::min(lo + 1, v.size() - 1);
+    return v[lo] + (v[hi] - v[lo]) * (pos - (double)lo);
+  };
+  out->p50_latency_ms = pct(h->latencies, 0.50);
+  out->p99_latency_ms = pct(h->latencies, 0.99);
+  out->p50_queue_ms = pct(h->queue_times, 0.50);
+  out->p99_queue_ms = pct(h->queue_times, 0.99);
   return DTWX_OK;
 }
 

@@ -16,6 +16,7 @@ arrival of a read's last needed chunk to its decision.
 """
 from __future__ import annotations
 
+import gc
 import heapq
 import time
 from dataclasses import dataclass
@@ -71,20 +72,23 @@ class SimulatedSequencer:
         self.reads = reads
         self.cfg = cfg
         self.rng = np.random.default_rng(cfg.seed + 2)
-        self.events = []            # (time_s, channel)
+        self.events = []            # (time_s, channel, generation)
+        self.gen = [0] * cfg.channels  # events of older generations are stale
         self.active = {}            # channel -> [read_number, pool index, next chunk k]
         self.next_read = 1
         self.truth = {}             # read_number -> target flag
         t0 = 0.0
         for ch in range(cfg.channels):
-            heapq.heappush(self.events, (t0 + self.rng.exponential(1.0 / cfg.read_rate), ch))
+            heapq.heappush(self.events, (t0 + self.rng.exponential(1.0 / cfg.read_rate), ch, 0))
 
     def due(self, now_s: float):
         """Chunks whose arrival time has come: (arrival_s, channel, read_number, samples, is_last)."""
         out = []
         cfg = self.cfg
         while self.events and self.events[0][0] <= now_s:
-            t, ch = heapq.heappop(self.events)
+            t, ch, g = heapq.heappop(self.events)
+            if g != self.gen[ch]:
+                continue
             st = self.active.get(ch)
             if st is None:  # a new read starts on this channel
                 idx = int(self.rng.integers(0, self.reads.n))
@@ -98,10 +102,10 @@ class SimulatedSequencer:
             out.append((t, ch, rn, x, last))
             st[2] += 1
             if not last:
-                heapq.heappush(self.events, (t + cfg.period_s, ch))
+                heapq.heappush(self.events, (t + cfg.period_s, ch, g))
             else:
                 self.active.pop(ch)
-                heapq.heappush(self.events, (t + cfg.period_s + self.rng.exponential(1.0 / cfg.read_rate), ch))
+                heapq.heappush(self.events, (t + cfg.period_s + self.rng.exponential(1.0 / cfg.read_rate), ch, g))
         return out
 
     def decided(self, ch: int, rn: int, now_s: float):
@@ -111,9 +115,8 @@ class SimulatedSequencer:
         st = self.active.get(ch)
         if st is not None and st[0] == rn:
             self.active.pop(ch)
-            self.events = [(t, c) for (t, c) in self.events if c != ch]
-            heapq.heapify(self.events)
-            heapq.heappush(self.events, (now_s + self.rng.exponential(1.0 / self.cfg.read_rate), ch))
+            self.gen[ch] += 1  # the channel's pending chunk event is dropped
+            heapq.heappush(self.events, (now_s + self.rng.exponential(1.0 / self.cfg.read_rate), ch, self.gen[ch]))
 
 
 def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget_bytes: float = 0.0,
@@ -129,8 +132,23 @@ def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget
     clf.serve_start(max_in_flight=max_in_flight, state_budget_bytes=state_budget_bytes,
                     chunks_per_decision=cfg.chunks_per_read, accept_per_sample=accept, reject_per_sample=reject)
     seq = SimulatedSequencer(reads, cfg)
+    # no garbage-collector pauses inside the real-time loop
+    gc_was_on = gc.isenabled()
+    gc.disable()
+    try:
+        rec = _loop(clf, seq, cfg, drain)
+    finally:
+        if gc_was_on:
+            gc.enable()
+    rec["accept_per_sample"], rec["reject_per_sample"] = accept, reject
+    return rec
+
+
+def _loop(clf, seq, cfg: ServeConfig, drain: bool) -> dict:
+    from . import now_ms
+
     t_base = now_ms()
-    lat, calls, truth = [], [], []
+    lat, queue, calls, truth = [], [], [], []
     decided_in_window = 0
     chunks_in_window = 0
     end_s = cfg.warmup_s + cfg.duration_s
@@ -149,6 +167,7 @@ def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget
                 if now_s >= cfg.warmup_s:
                     decided_in_window += 1
                     lat.append(d["latency_ms"])
+                    queue.append(d["queue_ms"])
                     calls.append(d["call"])
                     truth.append(seq.truth.get(d["read_number"], -1))
         time.sleep(0.00005)
@@ -156,6 +175,7 @@ def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget
     if drain:
         clf.serve_drain()
     lat = np.asarray(lat)
+    queue = np.asarray(queue)
     calls = np.asarray(calls)
     truth = np.asarray(truth)
     acc = float((calls == truth).mean()) if calls.size else float("nan")
@@ -166,6 +186,10 @@ def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget
         "p50_latency_ms": float(np.percentile(lat, 50)) if lat.size else None,
         "p99_latency_ms": float(np.percentile(lat, 99)) if lat.size else None,
         "max_latency_ms": float(lat.max()) if lat.size else None,
+        # latency = queue (arrival -> batch launch) + batch on the device + harvest
+        "p50_queue_ms": float(np.percentile(queue, 50)) if queue.size else None,
+        "p99_queue_ms": float(np.percentile(queue, 99)) if queue.size else None,
+        "p99_after_launch_ms": float(np.percentile(lat - queue, 99)) if lat.size else None,
         "call_accuracy": acc,
         "mean_batch_reads": st["mean_batch_reads"], "batches": st["batches"],
         "mean_batch_ms": st["mean_batch_ms"], "max_batch_ms": st["max_batch_ms"],
@@ -174,5 +198,4 @@ def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget
         "deferred_fraction": st["reads_deferred"] / max(seq.next_read - 1, 1),
         "queue_depth_end": st["queue_depth"],
         "state_bytes": st["state_bytes"],
-        "accept_per_sample": accept, "reject_per_sample": reject,
     }

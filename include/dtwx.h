@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define DTWX_ABI_VERSION 1
+#define DTWX_ABI_VERSION 2
 
 /* status codes */
 #define DTWX_OK 0
@@ -244,6 +244,7 @@ typedef struct dtwx_decision {
   int32_t chunks;    /* chunks aligned so far */
   int32_t samples;   /* samples aligned so far */
   double latency_ms; /* last needed chunk arrival -> decision */
+  double queue_ms;   /* that chunk's arrival -> launch of the batch that aligned it */
 } dtwx_decision;
 
 typedef struct dtwx_stats {
@@ -261,6 +262,8 @@ typedef struct dtwx_stats {
   double state_bytes;        /* device bytes of the row-state pool */
   double mean_batch_ms;      /* device time of a serving batch's sweep, mean and max */
   double max_batch_ms;
+  double p50_queue_ms;       /* decided reads: last chunk's arrival -> its batch launch */
+  double p99_queue_ms;
 } dtwx_stats;
 
 /* Prepare the handle for serving.  max_in_flight = reads holding device row

@@ -37,7 +37,7 @@ def test_python_binding_covers_header(built_lib):
 def test_config_default(built_lib):
     import dtwax_gb300 as d
     c = d.default_config()
-    assert c.abi_version == 1 and c.precision == d.FP16 and c.strand_mode == d.STRANDS_PAIRED
+    assert c.abi_version == 2 and c.precision == d.FP16 and c.strand_mode == d.STRANDS_PAIRED
     assert c.norm_eps == pytest.approx(1e-4)
     assert ctypes.sizeof(d.Config) == 96  # same static_assert in api.cpp
 
