@@ -305,6 +305,9 @@ def run_ours(args, rank, world, local):
         return float(t.item())
 
     precision = {"fp16": d.FP16, "fp32": d.FP32, "mixed": d.MIXED}[args.precision]
+    ref_del = args.recurrence == "ref_del"
+    if ref_del and precision != d.FP32:
+        raise SystemExit("--recurrence ref_del runs FP32 cells (--precision fp32)")
     w = synth.make_workload(args.workload, n_reads=args.reads or None)
     cells = w.cells()
     n_reads = w.reads.n
@@ -312,7 +315,7 @@ def run_ours(args, rank, world, local):
     use_graphs = 1 if (args.graphs or args.workload == "C3") else 0
     clf = d.Classifier(sequence=w.genome, level_table=w.table, precision=precision, device=local,
                        cells_per_thread=args.cells, chunk_strips=args.strips, warps_per_cta=args.warps,
-                       use_graphs=use_graphs)
+                       use_graphs=use_graphs, recurrence=d.REF_DEL if ref_del else d.NO_REF_DEL)
     if args.autotune or args.workload == "C3":
         clf.autotune(n_reads, int(np.diff(w.reads.offsets).mean()))
     stream = torch.cuda.Stream()
@@ -385,6 +388,8 @@ def run_ours(args, rank, world, local):
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     mhz = clock_rec.get("sm_mhz") or 2070.0
     per_sm_cycle = {d.FP16: 64.0, d.FP32: 128.0 / 3.0, d.MIXED: 128.0 / 2.5}[precision]
+    if ref_del:
+        per_sm_cycle = 128.0 / 9.0  # REF_DEL: 6 + 3 issue slots per cell in the two row passes
     theoretical = sms * per_sm_cycle * mhz * 1e6 / 1e9
     traffic = traffic_from_profile(args.precision)
     t_mask = w.reads.target == 1
@@ -395,7 +400,7 @@ def run_ours(args, rank, world, local):
         "data": "synthetic",
         "config": {"workload": f"{args.workload}: {WORKLOAD_DESC[args.workload]}", "cells_per_step": cells,
                    "reads_per_step": n_reads, "ref_columns_per_strand": w.ref_len,
-                   "precision": args.precision, "step": "window+z-score kernel, sDTW sweep, min/argmin finalize; "
+                   "precision": args.precision, "recurrence": args.recurrence, "step": "window+z-score kernel, sDTW sweep, min/argmin finalize; "
                    "raw samples resident in HBM", "l2": "flushed between timed steps (256 MB write)",
                    "tuning": tuning, "seeds": w.meta["seeds"], "parallelism": f"replicas x{world}"},
         "reads_per_s": reads_per_s,
@@ -438,6 +443,8 @@ def main():
     ap.add_argument("--skip-ref-gpu", action="store_true",
                     help="reference arm: do not time the reference's own GPU kernel beside the CPU line")
     ap.add_argument("--precision", choices=["fp16", "fp32", "mixed"], default="fp16")
+    ap.add_argument("--recurrence", choices=["no_ref_del", "ref_del"], default="no_ref_del",
+                    help="ref_del: the left predecessor of DTW.cu:23-29 (FP32 cells)")
     ap.add_argument("--reads", type=int, default=0,
                     help="use only the first N reads of the workload (small cases for profiling)")
     ap.add_argument("--skip-cpu", action="store_true", help="do not time the CPU baseline")

@@ -238,26 +238,31 @@ Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_row
   auto t = h->tuned.find(std::make_tuple(precision, log2_bucket((double)n_tasks), log2_bucket(mean_rows)));
   const bool use_t = t != h->tuned.end();
   // defaults measured on the 1 Mb / 2,048-read batch: 48 cells per lane (64 for
-  // MIXED, whose reference takes half the registers) in 4-warp CTAs
-  const int def_S = precision == 2 ? 64 : 48;
+  // MIXED, whose reference takes half the registers) in 4-warp CTAs; the REF_DEL
+  // instances have 16 or 32 cells per lane
+  const bool rd = h->cfg.recurrence == DTWX_REF_DEL;
+  const int def_S = rd ? 32 : (precision == 2 ? 64 : 48);
   s.S = o.S ? o.S : (f.S ? f.S : (use_t ? t->second.S : def_S));
   s.warps = o.warps ? o.warps : (f.warps ? f.warps : (use_t ? t->second.warps : 4));
   if (use_t && !f.G) g_scale = t->second.g_scale;
   if (o.S) g_scale = o.items > 0 ? o.items / 1000.0 : 1.0;  // candidate factor (per mille) while tuning
-  int occ = sdtw_ctas_per_sm(precision, s.S, s.warps);
+  int occ = sdtw_ctas_per_sm(precision, s.S, s.warps, rd);
   if (occ <= 0) occ = 1;
   const int W = kWarp * s.S;
   const int64_t strips = (h->m_cols + W - 1) / W;
   const int64_t total_warps = (int64_t)h->sms * occ * s.warps;
-  if (f.G && !o.S) {
+  const int strands = precision == 0 ? 1 : (h->cfg.strand_mode == DTWX_STRANDS_CONCAT ? 1 : 2);
+  if (rd) {
+    s.G = (int)strips;  // REF_DEL: one chunk per task (a horizontal run crosses any chunk edge)
+  } else if (f.G && !o.S) {
     s.G = f.G;
   } else {
-    const int g0 = choose_chunk_strips(strips, std::max<int64_t>(n_tasks, 1), mean_rows, W, total_warps);
+    const int g0 = choose_chunk_strips(strips, std::max<int64_t>(n_tasks, 1) * strands, mean_rows, W, total_warps);
     s.G = std::max(1, (int)std::lround(g0 * g_scale));
   }
   if (s.G > strips) s.G = (int)strips;
   const int64_t chunks = (strips + s.G - 1) / s.G;
-  const int64_t items = n_tasks * chunks;
+  const int64_t items = n_tasks * chunks * strands;
   s.items = (int)items;
   const int64_t want = (items + s.warps - 1) / s.warps;
   s.grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)h->sms * occ, want));
@@ -316,6 +321,7 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
     p.n_items = (int32_t)(n_tasks * p.n_chunks * (precision != 0 ? strands : 1));
     p.ref_layout = 1;
     p.strands = strands;
+    p.ref_del = h->cfg.recurrence == DTWX_REF_DEL ? 1 : 0;
     const int ii = inst_index(precision, sh.S);
     p.use_tma = h->tmap_ok[precision][ii] ? 1 : 0;
     // inside a stream capture the timing events become event-record nodes
@@ -577,6 +583,7 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
       p.chunk_strips = sh.G;
       p.max_rows = rows_cap;
       p.strands = h->cfg.strand_mode == DTWX_STRANDS_CONCAT ? 1 : 2;
+      p.ref_del = h->cfg.recurrence == DTWX_REF_DEL ? 1 : 0;
       p.n_items = p.n_chunks * (precision != 0 ? p.strands : 1);
       p.ref_layout = 1;
       const int ii = inst_index(precision, sh.S);
@@ -637,7 +644,12 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
     return fail(nullptr, DTWX_E_ARG, "bad precision");
   if (cfg.strand_mode != DTWX_STRANDS_PAIRED && cfg.strand_mode != DTWX_STRANDS_CONCAT)
     return fail(nullptr, DTWX_E_ARG, "bad strand_mode");
-  if (cfg.cells_per_thread && !sdtw_instance_exists(cfg.precision, cfg.cells_per_thread))
+  if (cfg.recurrence != DTWX_NO_REF_DEL && cfg.recurrence != DTWX_REF_DEL)
+    return fail(nullptr, DTWX_E_ARG, "bad recurrence");
+  if (cfg.recurrence == DTWX_REF_DEL && cfg.precision != DTWX_FP32)
+    return fail(nullptr, DTWX_E_ARG, "the REF_DEL recurrence is built for FP32 cells");
+  if (cfg.cells_per_thread &&
+      !sdtw_instance_exists(cfg.precision, cfg.cells_per_thread, cfg.recurrence == DTWX_REF_DEL))
     return fail(nullptr, DTWX_E_ARG, "cells_per_thread has no compiled kernel for this precision");
   if (cfg.warps_per_cta < 0 || cfg.warps_per_cta > 8) return fail(nullptr, DTWX_E_ARG, "warps_per_cta must be 1..8");
   if (cfg.chunk_strips < 0) return fail(nullptr, DTWX_E_ARG, "chunk_strips must be >= 0");
@@ -948,10 +960,13 @@ int dtwx_autotune(dtwx_handle *h, int32_t n_reads_req, int32_t read_len, float *
   cudaStream_t st = c.stream;
   struct Cand { int S, warps, permille; };
   std::vector<Cand> cands;
+  const bool rd = h->cfg.recurrence == DTWX_REF_DEL;
   for (int si = 0; si < inst_count(prec); ++si)
     for (int w : {4, 8})
       for (int pm : {500, 1000, 2000}) {
-        if (!sdtw_ctas_per_sm(prec, inst_S(prec, si), w)) continue;
+        if (!sdtw_instance_exists(prec, inst_S(prec, si), rd)) continue;
+        if (rd && pm != 1000) continue;  // one chunk per task: no chunk width to tune
+        if (!sdtw_ctas_per_sm(prec, inst_S(prec, si), w, rd)) continue;
         cands.push_back({inst_S(prec, si), w, pm});
       }
   float best = 1e30f;
@@ -999,7 +1014,10 @@ int dtwx_get_tuning(const dtwx_handle *h, int32_t *out, int32_t n) {
   if (!h || !out || n < 0) return DTWX_E_ARG;
   const Shape &s = h->last_shape[h->cfg.precision];
   const int32_t v[7] = {s.S, s.G, s.warps, s.grid, s.items,
-                        s.S ? sdtw_ctas_per_sm(h->cfg.precision, s.S, s.warps) : 0, (int32_t)h->graph_replays};
+                        s.S ? sdtw_ctas_per_sm(h->cfg.precision, s.S, s.warps,
+                                               h->cfg.recurrence == DTWX_REF_DEL)
+                            : 0,
+                        (int32_t)h->graph_replays};
   for (int i = 0; i < n && i < 7; ++i) out[i] = v[i];
   return DTWX_OK;
 }

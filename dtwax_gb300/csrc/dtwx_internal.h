@@ -60,6 +60,7 @@ struct SdtwParams {
   int32_t ref_layout;          // FP32: 0 = interleaved (fwd, rev) float pairs, 1 = planar (rev plane at m_pad);
                                // MIXED is always planar FP16
   int32_t strands;             // FP32/MIXED strands per task: 2 (paired), 1 (concatenated sequence); 0 = 2
+  int32_t ref_del;             // 1: REF_DEL recurrence (left predecessor); needs one chunk per task
 };
 
 // Per-warp scratch layout, in bytes, for cells of `pair_bytes` bytes.
@@ -101,15 +102,16 @@ __host__ __device__ inline float ordered_to_float(uint32_t o) {
 // ---------------------------------------------------------------- launchers
 // (defined in the .cu files; all return cudaError_t of the launch)
 
-// sDTW over all (task, chunk) items.  precision: 0 FP16, 1 FP32, 2 MIXED.
-// cells_per_thread must be one of the compiled instances.
+// sDTW over all (task, chunk) items.  precision: 0 FP16, 1 FP32, 2 MIXED;
+// p.ref_del selects the REF_DEL instances (FP32 only).  cells_per_thread must
+// be one of the compiled instances.
 cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, int grid,
                         const SdtwParams &p, const CUtensorMap *tmap, cudaStream_t s);
 // Dynamic shared memory the sDTW kernel needs per CTA.
 size_t sdtw_smem_bytes(int precision, int cells_per_thread, int warps_per_cta);
 // Resident CTAs per SM for the given shape (occupancy API), 0 on error.
-int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta);
-bool sdtw_instance_exists(int precision, int cells_per_thread);
+int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta, bool ref_del = false);
+bool sdtw_instance_exists(int precision, int cells_per_thread, bool ref_del = false);
 int sdtw_pair_bytes(int precision);  // bytes per DP cell (seam scratch)
 int sdtw_ref_bytes(int precision);   // reference bytes per column of a strip
 

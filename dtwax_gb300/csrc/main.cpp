@@ -19,6 +19,7 @@
 // Options:
 //   --fp32             FP32 cells (default FP16 half2 with running-min offset)
 //   --mixed            FP16 differences with FP32 path cost
+//   --ref-del          REF_DEL recurrence (left predecessor, FP32 cells)
 //   --threshold T      score below T calls "target" (default 194)
 //   --adapter N        samples skipped at the read start (default 1952, ADAPTER_LEN)
 //   --query-len N      samples aligned per read (default 2048, QUERY_LEN; 0 = rest)
@@ -156,7 +157,7 @@ bool load_txt(const std::string &path, std::vector<float> &out, std::string &err
 }
 
 int usage() {
-  std::cerr << "usage: dtwx_main <read_folder> <kmer_model> <ref.fasta> [--fp32|--mixed] [--threshold T]\n"
+  std::cerr << "usage: dtwx_main <read_folder> <kmer_model> <ref.fasta> [--fp32|--mixed] [--ref-del] [--threshold T]\n"
                "       [--adapter N] [--query-len N] [--allow-short] [--max-ref-len N] [--concat] [--side FILE]\n";
   return 2;
 }
@@ -185,6 +186,8 @@ int main(int argc, char **argv) {
       cfg.precision = DTWX_FP32;
     else if (a == "--mixed")
       cfg.precision = DTWX_MIXED;
+    else if (a == "--ref-del")
+      cfg.recurrence = DTWX_REF_DEL, cfg.precision = DTWX_FP32;
     else if (a == "--threshold")
       cfg.threshold = (float)atof(next());
     else if (a == "--adapter")

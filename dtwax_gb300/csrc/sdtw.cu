@@ -323,6 +323,55 @@ __device__ __forceinline__ void sweep_row_mixed(float (&D)[S], const __half2 (&R
   }
 }
 
+// The REF_DEL row (FP32 cells): the cell to the left in the same row is a
+// third predecessor, D[j] = min(v[j], c[j] + D[j-1]) with c = d^2 and
+// v = c + min(up, diag).  That is a scan along the row in the (min, +)
+// semiring, done in three passes:
+//  1. each lane runs its S columns with +inf entering on the left, keeping the
+//     local values P[j] in D and the lane's map x -> min(P[S-1], x + sum c);
+//  2. the 32 maps are composed by a warp scan, (a1, b1) then (a2, b2) being
+//     (a1 + a2, min(b2, b1 + a2)), which gives each lane its left input X;
+//  3. D[j] = min(P[j], X + c[0] + ... + c[j]).
+// seam_diag / seam_left are the left strip's last column on the previous and
+// on this row (lane 0 only).
+template <int S>
+__device__ __forceinline__ void sweep_row_refdel(float (&D)[S], const float (&R)[S], float q, float seam_diag,
+                                                 float seam_left, uint32_t m0, int lane) {
+  const float up = __shfl_up_sync(FULL_MASK, D[S - 1], 1);
+  float dprev = __uint_as_float((__float_as_uint(up) & ~m0) | (__float_as_uint(seam_diag) & m0));
+  float pacc = __int_as_float(0x7f800000), a = 0.f;
+#pragma unroll
+  for (int k = 0; k < S; ++k) {
+    const float top = D[k];
+    const float d = R[k] - q;
+    const float v = fmaf(d, d, fminf(top, dprev));
+    dprev = top;
+    pacc = fminf(v, fmaf(d, d, pacc));
+    a = fmaf(d, d, a);
+    D[k] = pacc;
+  }
+  float b = pacc;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const float ua = __shfl_up_sync(FULL_MASK, a, off);
+    const float ub = __shfl_up_sync(FULL_MASK, b, off);
+    const bool act = lane >= off;
+    b = act ? fminf(b, ub + a) : b;
+    a = act ? ua + a : a;
+  }
+  // exclusive prefix: the composed map of lanes 0..l-1 applied to seam_left
+  const float ea = __shfl_up_sync(FULL_MASK, a, 1);
+  const float eb = __shfl_up_sync(FULL_MASK, b, 1);
+  const float xin = fminf(eb, seam_left + ea);
+  float x = __uint_as_float((__float_as_uint(xin) & ~m0) | (__float_as_uint(seam_left) & m0));
+#pragma unroll
+  for (int k = 0; k < S; ++k) {
+    const float d = R[k] - q;
+    x = fmaf(d, d, x);
+    D[k] = fminf(D[k], x);
+  }
+}
+
 // Warp-wide lexicographic min of (value, column).
 __device__ __forceinline__ void warp_argmin(float &v, int64_t &j) {
 #pragma unroll
@@ -342,8 +391,6 @@ __device__ __forceinline__ unsigned long long make_key(float v, int64_t j) {
 
 // ---------------------------------------------------------------- the persistent kernel
 
-// Register cap per instance: the S cells and S reference elements of a lane
-// plus about 40 registers of bookkeeping, rounded to 128 or 168 (16 or 12 warps/SM).
 // One DP row for the policy: FP16 pairs and FP32 share sweep_row, MIXED has its own.
 template <int S, int PREC>
 __device__ __forceinline__ void row(typename Pol<PREC>::V (&D)[S],
@@ -355,12 +402,17 @@ __device__ __forceinline__ void row(typename Pol<PREC>::V (&D)[S],
     sweep_row<S, PREC>(D, R, qq, seam, m0);
 }
 
-template <int S, int PREC>
-constexpr int sdtw_reg_cap() { return S + S * Pol<PREC>::RB / 4 + 40 <= 128 ? 128 : 168; }
+// Register cap per instance: the S cells and S reference elements of a lane
+// plus about 40 registers of bookkeeping (70 for the REF_DEL scan), rounded to
+// 128 or 168 (16 or 12 warps/SM).
+template <int S, int PREC, bool RD>
+constexpr int sdtw_reg_cap() { return S + S * Pol<PREC>::RB / 4 + (RD ? 70 : 40) <= 128 ? 128 : 168; }
 
-template <int S, int PREC>
-__global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_constant__ CUtensorMap tmap,
-                                                                    const SdtwParams p) {
+// RD: the REF_DEL recurrence (FP32 cells).  A horizontal run can cross any
+// column chunk, so the host gives REF_DEL tasks one chunk (no halo).
+template <int S, int PREC, bool RD>
+__global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD>())) sdtw_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                                        const SdtwParams p) {
   using P = Pol<PREC>;
   using V = typename P::V;
   using RV = typename P::RV;
@@ -373,6 +425,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
   constexpr int K = kRescaleRows;
   static_assert(STRIP_BYTES % 1024 == 0, "strip tile must keep 1024-byte alignment");
   static_assert(S % 8 == 0, "row state and reference move in 16-byte groups");
+  static_assert(!RD || PREC == 1, "the REF_DEL row is built for FP32 cells");
 
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
@@ -555,21 +608,29 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
       // frame (delta changes only at a rescale, which ends a window)
       const V vinf = P::inf();
       typename P::QW qwin = P::qw(lane < n ? q[lane] : 0.f);
-      V swin = (!first && lane < rows) ? seam_in[lane] : vinf;
+      // REF_DEL also reads the seam value of the last row itself (one entry further)
+      constexpr int kExtra = RD ? 1 : 0;
+      V swin = (!first && lane < rows + kExtra) ? seam_in[lane] : vinf;
       if constexpr (PREC == 0) swin = __hadd2(swin, delta);
       V *so = seam_out + 1;  // seam value of row i goes to seam_out[i + 1]
       for (int i0 = 0; i0 < rows; i0 += kWarp) {
         const int r = i0 + kWarp + lane;
         const float qn = r < n ? q[r] : 0.f;
-        const V sn = (!first && r < rows) ? seam_in[r] : vinf;
+        const V sn = (!first && r < rows + kExtra) ? seam_in[r] : vinf;
         // the seam column leaving this strip is gathered in a register window
         // (lane l keeps row i0+l) and stored once per 32 rows, coalesced: no
         // lane-conditional store inside the row loop
         V sout = vinf;
+        // REF_DEL: lane l of lwin holds the left strip's value on row i0+l itself
+        V lwin = vinf;
+        if constexpr (RD) lwin = P::sel(lane == kWarp - 1, P::shfl(sn, 0), __shfl_down_sync(FULL_MASK, swin, 1));
         if (rows - i0 >= kWarp) {
 #pragma unroll 4
           for (int il = 0; il < kWarp; ++il) {
-            row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+            if constexpr (RD)
+              sweep_row_refdel<S>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
+            else
+              row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
             sout = P::sel(lane == il, P::shfl(D[S - 1], 31), sout);
           }
           if constexpr (PREC == 0) {
@@ -596,7 +657,10 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
         } else {
           const int cnt = rows - i0;
           for (int il = 0; il < cnt; ++il) {
-            row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+            if constexpr (RD)
+              sweep_row_refdel<S>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
+            else
+              row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
             sout = P::sel(lane == il, P::shfl(D[S - 1], 31), sout);
           }
           so[lane] = sout;  // lanes >= cnt write +inf into the buffer's 32-entry slack past the rows
@@ -671,11 +735,11 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(const __grid_
 
 // ---------------------------------------------------------------- instances / launch
 
-template <int S, int PREC>
+template <int S, int PREC, bool RD = false>
 static cudaError_t launch_inst(int warps, int grid, const SdtwParams &p, const CUtensorMap *tmap,
                                cudaStream_t s) {
   const size_t smem = sdtw_smem_bytes(PREC, S, warps);
-  auto fn = sdtw_kernel<S, PREC>;
+  auto fn = sdtw_kernel<S, PREC, RD>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   CUtensorMap dummy;
@@ -687,11 +751,11 @@ static cudaError_t launch_inst(int warps, int grid, const SdtwParams &p, const C
   return cudaGetLastError();
 }
 
-template <int S, int PREC>
+template <int S, int PREC, bool RD = false>
 static int occ_inst(int warps) {
   int n = 0;
   const size_t smem = sdtw_smem_bytes(PREC, S, warps);
-  auto fn = sdtw_kernel<S, PREC>;
+  auto fn = sdtw_kernel<S, PREC, RD>;
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, warps * kWarp, smem) != cudaSuccess) return 0;
@@ -707,7 +771,8 @@ size_t sdtw_smem_bytes(int precision, int cells_per_thread, int warps_per_cta) {
   return 1024 /* alignment slack */ + 2 * warps_per_cta * strip + 16 * warps_per_cta;
 }
 
-bool sdtw_instance_exists(int precision, int S) {
+bool sdtw_instance_exists(int precision, int S, bool ref_del) {
+  if (ref_del) return precision == 1 && (S == 16 || S == 32);
   if (precision == 0) return S == 32 || S == 48;
   if (precision == 2) return S == 32 || S == 48 || S == 64;
   return S == 16 || S == 32 || S == 48;
@@ -715,9 +780,16 @@ bool sdtw_instance_exists(int precision, int S) {
 
 #define DTWX_DISPATCH(PREC, S, CALL) \
   if (precision == PREC && cells_per_thread == S) return CALL<S, PREC>
+#define DTWX_DISPATCH_RD(S, CALL) \
+  if (precision == 1 && cells_per_thread == S) return CALL<S, 1, true>
 
 cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, int grid,
                         const SdtwParams &p, const CUtensorMap *tmap, cudaStream_t s) {
+  if (p.ref_del) {
+    DTWX_DISPATCH_RD(16, launch_inst)(warps_per_cta, grid, p, tmap, s);
+    DTWX_DISPATCH_RD(32, launch_inst)(warps_per_cta, grid, p, tmap, s);
+    return cudaErrorInvalidValue;
+  }
   DTWX_DISPATCH(0, 32, launch_inst)(warps_per_cta, grid, p, tmap, s);
   DTWX_DISPATCH(0, 48, launch_inst)(warps_per_cta, grid, p, tmap, s);
   DTWX_DISPATCH(1, 16, launch_inst)(warps_per_cta, grid, p, tmap, s);
@@ -729,7 +801,12 @@ cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, 
   return cudaErrorInvalidValue;
 }
 
-int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta) {
+int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta, bool ref_del) {
+  if (ref_del) {
+    DTWX_DISPATCH_RD(16, occ_inst)(warps_per_cta);
+    DTWX_DISPATCH_RD(32, occ_inst)(warps_per_cta);
+    return 0;
+  }
   DTWX_DISPATCH(0, 32, occ_inst)(warps_per_cta);
   DTWX_DISPATCH(0, 48, occ_inst)(warps_per_cta);
   DTWX_DISPATCH(1, 16, occ_inst)(warps_per_cta);

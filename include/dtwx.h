@@ -44,6 +44,12 @@ extern "C" {
 #define DTWX_MIXED 2 /* FP16 differences (half2: two columns of one strand), FP32 cells:
                         each cell is one f32 = f16*f16 + f32 FMA */
 
+/* the recurrence */
+#define DTWX_NO_REF_DEL 0 /* D = d^2 + min(up, diag): the reference's build (-DNO_REF_DEL, src/Makefile:8) */
+#define DTWX_REF_DEL 1    /* D = d^2 + min(left, up, diag) (DTW.cu:23-29 without -DNO_REF_DEL);
+                             FP32 cells only; a read is one work item per strand (a
+                             horizontal run can cross any column chunk) */
+
 /* how the two strands are scored */
 #define DTWX_STRANDS_PAIRED 0 /* fwd and rev aligned separately (DTW.cu half2 .x/.y) */
 #define DTWX_STRANDS_CONCAT 1 /* one sequence fwd||rev (load_reference.hpp:36-37, sdtw.py:234) */
@@ -72,7 +78,8 @@ typedef struct dtwx_config {
                               repeats (same buffers, offsets and stream): the first such batch runs
                               directly, the second is captured, later ones are replays */
   int32_t serve_batches;   /* serving batches in flight at once (1..4), 0 = 2 */
-  int32_t reserved[6];
+  int32_t recurrence;      /* DTWX_NO_REF_DEL (default) or DTWX_REF_DEL */
+  int32_t reserved[5];
 } dtwx_config;
 
 /* Per-read outcome.  end_pos is the DP column (0-based k-mer position on the

@@ -61,6 +61,11 @@ def lib():
         L.oracle_sdtw_batch.argtypes = [_d, _d, ctypes.c_int64, _d, _i64, ctypes.c_int,
                                         _d, _i64, _d, _i64, ctypes.c_int]
         L.oracle_sdtw_batch.restype = None
+        L.oracle_sdtw_ref_del.argtypes = [_d, ctypes.c_int64, _d, ctypes.c_int64, _d, _d, _i64]
+        L.oracle_sdtw_ref_del.restype = ctypes.c_double
+        L.oracle_sdtw_batch_rec.argtypes = [_d, _d, ctypes.c_int64, _d, _i64, ctypes.c_int,
+                                            _d, _i64, _d, _i64, ctypes.c_int, ctypes.c_int]
+        L.oracle_sdtw_batch_rec.restype = None
         L.oracle_sdtw_refkernel.argtypes = [_d, ctypes.c_int64, _d, ctypes.c_int64, ctypes.c_int]
         L.oracle_sdtw_refkernel.restype = ctypes.c_double
         L.oracle_sdtw_refkernel_batch.argtypes = [_d, ctypes.c_int64, _d, ctypes.c_int64, ctypes.c_int,
@@ -137,8 +142,22 @@ def sdtw(ref, q, init_row=None, trace_cols=None, want_row: bool = False):
     return tuple(out)
 
 
-def sdtw_batch(fwd, rev, queries, offsets, n_threads: int = 0):
-    """Per read: (score_fwd, end_fwd, score_rev, end_rev) arrays, FP64, OpenMP."""
+def sdtw_ref_del(ref, q, init_row=None, want_row: bool = False):
+    """FP64 sDTW with the REF_DEL recurrence (a left predecessor in the same
+    row, DTW.cu:23-29): (score, argmin[, final row])."""
+    ref = np.ascontiguousarray(ref, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    am = np.zeros(1, np.int64)
+    init = None if init_row is None else np.ascontiguousarray(init_row, dtype=np.float64)
+    row = np.empty(ref.size, np.float64) if want_row else None
+    s = lib().oracle_sdtw_ref_del(_dp(ref), ref.size, _dp(q), q.size, _dp(init) if init is not None else None,
+                                  _dp(row) if row is not None else None, _ip(am))
+    return (float(s), int(am[0]), row) if want_row else (float(s), int(am[0]))
+
+
+def sdtw_batch(fwd, rev, queries, offsets, n_threads: int = 0, ref_del: bool = False):
+    """Per read: (score_fwd, end_fwd, score_rev, end_rev) arrays, FP64, OpenMP;
+    ref_del selects the REF_DEL recurrence."""
     fwd = np.ascontiguousarray(fwd, dtype=np.float64)
     rev = np.ascontiguousarray(rev, dtype=np.float64)
     assert fwd.size == rev.size
@@ -150,8 +169,8 @@ def sdtw_batch(fwd, rev, queries, offsets, n_threads: int = 0):
     ef = np.empty(n, np.int64)
     er = np.empty(n, np.int64)
     if n > 0:
-        lib().oracle_sdtw_batch(_dp(fwd), _dp(rev), fwd.size, _dp(queries), _ip(offsets), n,
-                                _dp(sf), _ip(ef), _dp(sr), _ip(er), int(n_threads))
+        lib().oracle_sdtw_batch_rec(_dp(fwd), _dp(rev), fwd.size, _dp(queries), _ip(offsets), n,
+                                    _dp(sf), _ip(ef), _dp(sr), _ip(er), int(n_threads), int(bool(ref_del)))
     return sf, ef, sr, er
 
 
@@ -163,6 +182,7 @@ REFK_CHUNK_SEAM_DIAG = 1
 REFK_CHUNK_LANE1_DIAG = 2
 REFK_SEAM_SHIFT = 4
 REFK_ALL = 7
+REFK_REF_DEL = 8  # the REF_DEL recurrence (not a departure)
 
 
 def sdtw_refkernel(ref, q, quirks: int = REFK_ALL) -> float:
@@ -250,8 +270,9 @@ def np_build_levels(seq: bytes, table, cap: int = 0):
     return out[0], out[1]
 
 
-def np_sdtw(ref, q, init_row=None):
-    """Row-vectorised FP64 sDTW for small cases (sdtw.py:205-225)."""
+def np_sdtw(ref, q, init_row=None, ref_del: bool = False):
+    """Row-vectorised FP64 sDTW for small cases (sdtw.py:205-225); ref_del
+    adds the left predecessor (DTW.cu:23-29) with a plain loop along the row."""
     ref = np.asarray(ref, dtype=np.float64)
     q = np.asarray(q, dtype=np.float64)
     prev = np.zeros(ref.size) if init_row is None else np.array(init_row, dtype=np.float64)
@@ -260,6 +281,9 @@ def np_sdtw(ref, q, init_row=None):
         cur = np.empty_like(prev)
         cur[0] = cost[0] + prev[0]
         cur[1:] = cost[1:] + np.minimum(prev[1:], prev[:-1])
+        if ref_del:
+            for j in range(1, ref.size):
+                cur[j] = min(cur[j], cost[j] + cur[j - 1])
         prev = cur
     j = int(np.argmin(prev))
     return float(prev[j]), j, prev

@@ -17,7 +17,8 @@
 // which comes from -DHARNESS_REF_LEN so one cubin exists per reference
 // geometry (common.hpp:60-67 fixes it at 47*1024 per strand for FP16 and
 // 2*47*1024 for FP32).  Build flags follow src/Makefile:8 (-DNO_REF_DEL, and
-// -DFP16 for the half2 build).
+// -DFP16 for the half2 build); without -DNO_REF_DEL the kernel carries the
+// REF_DEL recurrence (DTW.cu:23-29).
 //
 // <cuda_fp16.h> and <cooperative_groups.h> are included at file scope first:
 // DTW.cu includes them again inside namespace FullDTW, where a first inclusion

@@ -6,8 +6,9 @@ product package (dtwax_gb300) never does.
 
 * ``build()`` compiles oracle/ref_dtw_harness.cu, which includes the
   reference's unmodified src/include/DTW.hpp + DTW.cu (FullDTW::DTW,
-  DTW.cu:151-572, with -DNO_REF_DEL as src/Makefile:8 sets it), into one
-  device-only cubin per reference geometry under oracle/_ref/.  It needs the
+  DTW.cu:151-572, with -DNO_REF_DEL as src/Makefile:8 sets it, or without it
+  for the REF_DEL recurrence), into one device-only cubin per reference
+  geometry under oracle/_ref/.  It needs the
   reference's sources, so it runs only where they are (this build container);
   the cubins travel with the repository and nothing else of the reference does.
 * ``RefKernel`` loads a cubin through the CUDA driver API (ctypes on
@@ -50,14 +51,19 @@ QUERY_LEN = 2048      # common.hpp:58
 BLOCK_NUM = 10        # reads per launch in main.cu (common.hpp:68)
 DYN_SMEM = 256
 
-# name -> (precision, REF_LEN).  FP16: REF_LEN columns per strand (fwd in .x,
-# rev in .y of one half2); FP32: fwd then rev concatenated (load_reference.hpp:36-37).
+# name -> (precision, REF_LEN, ref_del).  FP16: REF_LEN columns per strand (fwd
+# in .x, rev in .y of one half2); FP32: fwd then rev concatenated
+# (load_reference.hpp:36-37).  ref_del: built without -DNO_REF_DEL, i.e. with
+# the left predecessor of DTW.cu:23-29 (names ending in _rd).
 GEOMETRIES = {
-    "fp16_4160": ("fp16", 4160),          # 5 tiles per strand
-    "fp16_48128": ("fp16", 48128),        # the shipped FP16 shape, 47*1024 (57 tiles scored)
-    "fp16_1000064": ("fp16", 1000064),    # 1,202 tiles: a 1 Mb genome (999,995 columns per strand)
-    "fp32_8320": ("fp32", 8320),          # 2 x 4,160 concatenated
-    "fp32_94848": ("fp32", 94848),        # 2 x 47,424 concatenated (114 tiles)
+    "fp16_4160": ("fp16", 4160, False),          # 5 tiles per strand
+    "fp16_48128": ("fp16", 48128, False),        # the shipped FP16 shape, 47*1024 (57 tiles scored)
+    "fp16_1000064": ("fp16", 1000064, False),    # 1,202 tiles: a 1 Mb genome (999,995 columns per strand)
+    "fp32_8320": ("fp32", 8320, False),          # 2 x 4,160 concatenated
+    "fp32_94848": ("fp32", 94848, False),        # 2 x 47,424 concatenated (114 tiles)
+    "fp16_4160_rd": ("fp16", 4160, True),
+    "fp16_48128_rd": ("fp16", 48128, True),
+    "fp32_8320_rd": ("fp32", 8320, True),
 }
 
 # Kernel symbols of the two instantiations (as ptxas -v reports them when the
@@ -81,10 +87,12 @@ def sources_present() -> bool:
 
 
 def _compile(name: str) -> str:
-    prec, ref_len = GEOMETRIES[name]
+    prec, ref_len, ref_del = GEOMETRIES[name]
     out = cubin_path(name)
     cmd = ["nvcc", "-cubin", "-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a",
-           "-DNO_REF_DEL", f"-DHARNESS_REF_LEN={ref_len}", "-I", REFERENCE_INCLUDE]
+           f"-DHARNESS_REF_LEN={ref_len}", "-I", REFERENCE_INCLUDE]
+    if not ref_del:
+        cmd.append("-DNO_REF_DEL")
     if prec == "fp16":
         cmd.append("-DFP16")
     cmd += [HARNESS, "-o", out + ".tmp"]
@@ -162,7 +170,7 @@ class RefKernel:
         if not available(name):
             raise FileNotFoundError(f"{cubin_path(name)} not built (needs the reference's sources at build time)")
         self.name = name
-        self.precision, self.ref_len = GEOMETRIES[name]
+        self.precision, self.ref_len, self.ref_del = GEOMETRIES[name]
         self.tiles = self.ref_len // TILE
         self.scored = self.tiles * TILE
         torch.zeros(1, device="cuda")  # make the primary context current

@@ -138,9 +138,28 @@ int64_t oracle_build_levels(const char *seq, int64_t L, const double *table,
  * final_row (nullable, length m) receives D[n-1][*].
  * trace_cols/trace_out (nullable) record D[i][trace_cols[t]] for every row
  * into trace_out[i*n_trace + t], the layout of the golden log. */
+static double sdtw_rows(const double *ref, int64_t m, const double *q, int64_t n,
+                        const double *init_row, double *final_row, int64_t *argmin,
+                        const int64_t *trace_cols, int n_trace, double *trace_out, int ref_del);
+
 double oracle_sdtw(const double *ref, int64_t m, const double *q, int64_t n,
                    const double *init_row, double *final_row, int64_t *argmin,
                    const int64_t *trace_cols, int n_trace, double *trace_out) {
+  return sdtw_rows(ref, m, q, n, init_row, final_row, argmin, trace_cols, n_trace, trace_out, 0);
+}
+
+/* The REF_DEL recurrence of the reference's kernel built without -DNO_REF_DEL
+ * (src/include/DTW.cu:23-29): a third predecessor, the cell to the left in the
+ * same row, D[i][j] = d^2 + min(D[i][j-1], D[i-1][j], D[i-1][j-1]).  Row 0 is
+ * the cost alone (the free start's zero row above wins every minimum). */
+double oracle_sdtw_ref_del(const double *ref, int64_t m, const double *q, int64_t n,
+                           const double *init_row, double *final_row, int64_t *argmin) {
+  return sdtw_rows(ref, m, q, n, init_row, final_row, argmin, NULL, 0, NULL, 1);
+}
+
+static double sdtw_rows(const double *ref, int64_t m, const double *q, int64_t n,
+                        const double *init_row, double *final_row, int64_t *argmin,
+                        const int64_t *trace_cols, int n_trace, double *trace_out, int ref_del) {
   if (m <= 0 || n <= 0) {
     if (argmin) *argmin = -1;
     return INFINITY;
@@ -163,7 +182,9 @@ double oracle_sdtw(const double *ref, int64_t m, const double *q, int64_t n,
     for (int64_t j = 1; j < m; ++j) {
       double d = ref[j] - qi;
       double a = prev[j], b = prev[j - 1];
-      cur[j] = d * d + (a < b ? a : b);
+      double mn = a < b ? a : b;
+      if (ref_del && cur[j - 1] < mn) mn = cur[j - 1];
+      cur[j] = d * d + mn;
     }
     if (trace_out)
       for (int t = 0; t < n_trace; ++t) trace_out[i * n_trace + t] = cur[trace_cols[t]];
@@ -184,10 +205,24 @@ double oracle_sdtw(const double *ref, int64_t m, const double *q, int64_t n,
  * queries holds the normalised reads back to back; read r is
  * queries[offsets[r] .. offsets[r+1]).  Outputs per read and strand:
  * min score and smallest end column.  n_threads <= 0 uses all cores. */
+void oracle_sdtw_batch_rec(const double *fwd, const double *rev, int64_t m,
+                           const double *queries, const int64_t *offsets, int n_reads,
+                           double *score_fwd, int64_t *end_fwd, double *score_rev,
+                           int64_t *end_rev, int n_threads, int ref_del);
+
 void oracle_sdtw_batch(const double *fwd, const double *rev, int64_t m,
                        const double *queries, const int64_t *offsets, int n_reads,
                        double *score_fwd, int64_t *end_fwd, double *score_rev,
                        int64_t *end_rev, int n_threads) {
+  oracle_sdtw_batch_rec(fwd, rev, m, queries, offsets, n_reads, score_fwd, end_fwd, score_rev, end_rev,
+                        n_threads, 0);
+}
+
+/* oracle_sdtw_batch with the recurrence chosen: ref_del 0 (NO_REF_DEL) or 1. */
+void oracle_sdtw_batch_rec(const double *fwd, const double *rev, int64_t m,
+                           const double *queries, const int64_t *offsets, int n_reads,
+                           double *score_fwd, int64_t *end_fwd, double *score_rev,
+                           int64_t *end_rev, int n_threads, int ref_del) {
 #ifdef _OPENMP
   if (n_threads > 0) omp_set_num_threads(n_threads);
 #endif
@@ -199,7 +234,7 @@ void oracle_sdtw_batch(const double *fwd, const double *rev, int64_t m,
     const double *q = queries + offsets[r];
     const int64_t n = offsets[r + 1] - offsets[r];
     int64_t am = -1;
-    double s = oracle_sdtw(strand == 0 ? fwd : rev, m, q, n, NULL, NULL, &am, NULL, 0, NULL);
+    double s = sdtw_rows(strand == 0 ? fwd : rev, m, q, n, NULL, NULL, &am, NULL, 0, NULL, ref_del);
     if (strand == 0) { score_fwd[r] = s; end_fwd[r] = am; }
     else { score_rev[r] = s; end_rev[r] = am; }
   }
@@ -225,6 +260,11 @@ void oracle_sdtw_batch(const double *fwd, const double *rev, int64_t m,
  *   REFK_SEAM_SHIFT (4): seam rows 961..991 written by a middle tile hold the
  *     value of the row 31 below (the write index wave - 63 at DTW.cu:387
  *     against wave - 32 in the first tile, DTW.cu:267), seen by the next tile.
+ * REFK_REF_DEL (8) is not a departure but the recurrence of the kernel built
+ * without -DNO_REF_DEL (DTW.cu:23-29): the cell to the left in the same row is
+ * a third predecessor; a tile's first column takes it from the seam buffer
+ * (penalty_left = penalty_last_col[wave], DTW.cu:384, :516), so the seam shift
+ * reaches it too.
  * m must be a multiple of 832 with at least two tiles (the kernel's own
  * geometry, its last partial tile is never scored) and n a multiple of 1024.
  * Returns min_j D[n-1][j] (the kernel reports no column), or NaN on a bad
@@ -235,6 +275,7 @@ void oracle_sdtw_batch(const double *fwd, const double *rev, int64_t m,
 #define REFK_CHUNK_SEAM_DIAG 1
 #define REFK_CHUNK_LANE1_DIAG 2
 #define REFK_SEAM_SHIFT 4
+#define REFK_REF_DEL 8
 
 double oracle_sdtw_refkernel(const double *ref, int64_t m, const double *q, int64_t n, int quirks) {
   if (m < 2 * REFK_TILE || m % REFK_TILE != 0 || n <= 0 || n % REFK_CHUNK != 0) return NAN;
@@ -272,7 +313,12 @@ double oracle_sdtw_refkernel(const double *ref, int64_t m, const double *q, int6
           else
             diag = seam_prev[r - 1];
           if (r == 0 && j == REFK_LANE_CELLS && (quirks & REFK_CHUNK_LANE1_DIAG)) diag = INFINITY;
-          cur[j] = cost + (top < diag ? top : diag);
+          double mn = top < diag ? top : diag;
+          if (quirks & REFK_REF_DEL) {
+            const double left = j > 0 ? cur[j - 1] : (k == 0 ? INFINITY : seam_prev[r]);
+            if (left < mn) mn = left;
+          }
+          cur[j] = cost + mn;
         }
         seam_cur[r] = cur[REFK_TILE - 1];
         if (r == REFK_CHUNK - 1) memcpy(last_out + c0, cur, sizeof(double) * REFK_TILE);

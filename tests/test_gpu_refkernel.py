@@ -146,6 +146,63 @@ def test_concat_mode_matches_refkernel_fp32(small, oracle, built_lib):
     assert rel(ours[same], theirs[same]).max() <= 2e-5
 
 
+def test_refkernel_ref_del_matches_model(small, oracle):
+    """The reference kernel built without -DNO_REF_DEL (left predecessor,
+    DTW.cu:23-29) against the same FP64 model with the REF_DEL switch: FP32
+    within 1e-5, FP16 within its accumulation error; without the switch the
+    model misses the kernel."""
+    need("fp32_8320_rd")
+    need("fp16_4160_rd")
+    fwd, rev, z, crafted, junction = small
+    cat = np.concatenate([fwd, rev]).astype(np.float64)
+    q = np.concatenate([z, crafted, junction[None]])
+    with RK.RefKernel("fp32_8320_rd") as k:
+        got = k.run(k.reference(fwd, rev), q)
+    model = oracle.sdtw_refkernel_batch(cat, q.astype(np.float64), oracle.REFK_ALL | oracle.REFK_REF_DEL)
+    no_left = oracle.sdtw_refkernel_batch(cat, q.astype(np.float64), oracle.REFK_ALL)
+    e = rel(got, model)
+    print(f"\nREF_DEL FP32 reference kernel vs FP64 model: max rel {e.max():.2e}; "
+          f"vs the model without the left term: max rel {rel(got, no_left).max():.2e}")
+    assert e.max() <= 1e-5
+    assert (rel(got, no_left) > 1e-3).any()
+    q16s = np.concatenate([z, crafted])
+    with RK.RefKernel("fp16_4160_rd") as k:
+        gf, gr = k.run(k.reference(fwd, rev), q16s)
+    f16 = fwd.astype(np.float16).astype(np.float64)
+    r16 = rev.astype(np.float16).astype(np.float64)
+    q16 = q16s.astype(np.float16).astype(np.float64)
+    mf = oracle.sdtw_refkernel_batch(f16, q16, oracle.REFK_ALL | oracle.REFK_REF_DEL)
+    mr = oracle.sdtw_refkernel_batch(r16, q16, oracle.REFK_ALL | oracle.REFK_REF_DEL)
+    e16 = max(rel(gf, mf).max(), rel(gr, mr).max())
+    print(f"REF_DEL FP16 reference kernel vs FP64 model (half inputs): max rel {e16:.2e}")
+    assert e16 <= 0.08
+
+
+def test_ref_del_concat_matches_refkernel_fp32(small, oracle, built_lib):
+    """This library's REF_DEL FP32 cells on the concatenated strands against
+    the reference's REF_DEL FP32 kernel, on reads the departures leave alone."""
+    need("fp32_8320_rd")
+    import dtwax_gb300 as d
+    fwd, rev, z, _, _ = small
+    g = synth.random_genome(5 * TILE + 5, 1)
+    o = synth.random_genome(5 * TILE + 5, 2)
+    table = synth.level_table()
+    reads = synth.simulate_reads(g, o, table, [QLEN] * 16, (np.arange(16) % 2 == 0).astype(np.int8), seed=5)
+    with make_classifier(g, table, precision=d.FP32, strand_mode=d.STRANDS_CONCAT, recurrence=d.REF_DEL) as clf:
+        ours = clf.classify(raw=reads.raw, offsets=reads.offsets)["score"]
+    cat = np.concatenate([fwd, rev]).astype(np.float64)
+    exact = oracle.sdtw_refkernel_batch(cat, z.astype(np.float64), oracle.REFK_REF_DEL)
+    model = oracle.sdtw_refkernel_batch(cat, z.astype(np.float64), oracle.REFK_ALL | oracle.REFK_REF_DEL)
+    with RK.RefKernel("fp32_8320_rd") as k:
+        theirs = k.run(k.reference(fwd, rev), z)
+    same = model == exact
+    print(f"\nREF_DEL concat FP32: {same.sum()} of {same.size} reads unaffected by the departures; "
+          f"ours vs reference kernel max rel {rel(ours[same], theirs[same]).max():.2e}")
+    assert rel(ours, exact).max() <= 1e-5
+    assert same.sum() >= 8
+    assert rel(ours[same], theirs[same]).max() <= 2e-5
+
+
 @pytest.fixture(scope="module")
 def c1_tiles(built_lib, oracle):
     """C1 shape on whole tiles: a 47,429-base genome (47,424 = 57 x 832

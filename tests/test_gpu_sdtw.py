@@ -110,6 +110,43 @@ def test_classify_matches_oracle(lib, oracle, genome_pair, precision):
                 assert abs(int(res["end_pos"][i]) - int(best_end)) <= 1
 
 
+@pytest.mark.parametrize("cells,warps", [(16, 4), (32, 4), (32, 8), (16, 1)])
+def test_ref_del_matches_oracle(lib, oracle, genome_pair, cells, warps):
+    """The REF_DEL recurrence (left predecessor, DTW.cu:23-29) in FP32 cells
+    against the FP64 oracle, on reads of window-edge lengths."""
+    import dtwax_gb300 as d
+    g, o = genome_pair
+    tab = synth.level_table()
+    lengths = [2000, 1, 2, 31, 32, 33, 1023, 1024, 1025, 2047, 2049, 3000, 500, 777]
+    reads = reads_of_lengths(g, o, tab, lengths)
+    with make_classifier(g, tab, precision=d.FP32, recurrence=d.REF_DEL, cells_per_thread=cells,
+                         warps_per_cta=warps) as clf:
+        res = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        t = clf.tuning()
+        fwd, rev = clf.reference()
+    assert t["cells_per_thread"] == cells and t["work_items"] == 2 * len(lengths)  # one chunk per read strand
+    qs, offs = [], [0]
+    for r in range(reads.n):
+        z = oracle.zscore(reads.read(r).astype(np.float64), 1e-4).astype(np.float32).astype(np.float64)
+        qs.append(z)
+        offs.append(offs[-1] + z.size)
+    ora = oracle.sdtw_batch(fwd.astype(np.float64), rev.astype(np.float64), np.concatenate(qs),
+                            np.array(offs, np.int64), ref_del=True)
+    check_fp32(res, ora)
+    # the left term matters on these reads: NO_REF_DEL scores differ
+    plain = oracle.sdtw_batch(fwd.astype(np.float64), rev.astype(np.float64), np.concatenate(qs),
+                              np.array(offs, np.int64))
+    assert (plain[0] > ora[0]).any()
+
+
+def test_ref_del_rejects_other_cells(lib, genome_pair):
+    import dtwax_gb300 as d
+    g, _ = genome_pair
+    for prec in (d.FP16, d.MIXED):
+        with pytest.raises(d.DtwxError):
+            make_classifier(g, synth.level_table(), precision=prec, recurrence=d.REF_DEL)
+
+
 @pytest.mark.parametrize("cells,strips,warps", [(16, 1, 8), (32, 3, 2), (48, 2, 4), (32, 50, 1)])
 def test_fp32_chunking_is_exact(lib, genome_pair, cells, strips, warps):
     """Chunks recompute a halo, so any chunk size gives the same FP32 bits."""

@@ -15,14 +15,15 @@ from dtwax_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 
-def oracle_decisions(oracle, fwd, rev, chunks):
+def oracle_decisions(oracle, fwd, rev, chunks, ref_del=False):
     """Best hit after each chunk, resumed from the saved rows."""
     out = []
     rf = rr = None
+    run = oracle.sdtw_ref_del if ref_del else oracle.sdtw
     for c in chunks:
         z = oracle.zscore(c.astype(np.float64), 1e-4).astype(np.float32).astype(np.float64)
-        sf, ef, rf = oracle.sdtw(fwd, z, init_row=rf, want_row=True)
-        sr, er, rr = oracle.sdtw(rev, z, init_row=rr, want_row=True)
+        sf, ef, rf = run(fwd, z, init_row=rf, want_row=True)
+        sr, er, rr = run(rev, z, init_row=rr, want_row=True)
         score, end, strand = oracle.combine([sf], [ef], [sr], [er])
         out.append((float(score[0]), int(end[0]), int(strand[0])))
     return out
@@ -82,6 +83,21 @@ def test_resume_matches_oracle(setup, oracle, precision, rtol):
             assert d["score"] == pytest.approx(s, rel=rtol)
             if precision == 1:
                 assert (d["end_pos"], d["strand"]) == (e, st)
+
+
+def test_resume_ref_del_matches_oracle(setup, oracle):
+    """The REF_DEL recurrence resumed chunk by chunk from the saved rows."""
+    import dtwax_gb300 as d
+    g, o, tab, reads = setup
+    with make_classifier(g, tab, precision=d.FP32, recurrence=d.REF_DEL, threshold=-1.0) as clf:
+        fwd, rev = clf.reference()
+        chunks = {i: split(reads.read(i), 1600) for i in range(reads.n)}
+        got = serve_reads(clf, chunks, chunks_per_decision=3)
+    for i in range(reads.n):
+        want = oracle_decisions(oracle, fwd.astype(np.float64), rev.astype(np.float64), chunks[i][:3], ref_del=True)
+        for dd, (s, e, st) in zip(got[i], want):
+            assert dd["score"] == pytest.approx(s, rel=1e-5)
+            assert (dd["end_pos"], dd["strand"]) == (e, st)
 
 
 @pytest.mark.parametrize("precision", [1, 0, 2])

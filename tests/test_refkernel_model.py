@@ -18,6 +18,24 @@ def test_tile_order_without_departures_is_the_recurrence(oracle, tiles):
     for n in (1024, 2048, 3072):
         q = rng.standard_normal(n)
         assert oracle.sdtw_refkernel(ref, q, 0) == oracle.sdtw(ref, q)[0]
+        assert oracle.sdtw_refkernel(ref, q, oracle.REFK_REF_DEL) == oracle.sdtw_ref_del(ref, q)[0]
+
+
+def test_ref_del_oracle_matches_numpy(oracle):
+    """The C REF_DEL recurrence against the plain numpy loop, and the left
+    term can only lower a score."""
+    rng = np.random.default_rng(11)
+    for m, n in ((40, 7), (300, 50), (1000, 120)):
+        ref = rng.standard_normal(m)
+        q = rng.standard_normal(n)
+        s, j = oracle.sdtw_ref_del(ref, q)
+        s_np, j_np, _ = oracle.np_sdtw(ref, q, ref_del=True)
+        assert s == pytest.approx(s_np, rel=1e-12) and j == j_np
+        assert s <= oracle.sdtw(ref, q)[0]
+        init = rng.random(m) * 5
+        s2, _, row = oracle.sdtw_ref_del(ref, q, init_row=init, want_row=True)
+        s2_np, _, row_np = oracle.np_sdtw(ref, q, init_row=init, ref_del=True)
+        np.testing.assert_allclose(row, row_np, rtol=1e-12)
 
 
 def test_each_departure_acts_where_expected(oracle):
