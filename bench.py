@@ -165,7 +165,8 @@ SERVING = {
 }
 
 
-def run_serving(name: str, precision: int, device: int, duration_s: float, batches: int = 0):
+def run_serving(name: str, precision: int, device: int, duration_s: float, batches: int = 0,
+                state: str = "fp32"):
     import dtwax_gb300 as d
     from dtwax_gb300 import readuntil, synth
 
@@ -175,14 +176,16 @@ def run_serving(name: str, precision: int, device: int, duration_s: float, batch
     tab = synth.level_table()
     cfg = readuntil.ServeConfig(channels=spec["channels"], duration_s=duration_s, warmup_s=2.0)
     reads = readuntil.make_pool(g, o, tab, cfg)
+    state_precision = d.STATE_FP16 if state == "fp16" and precision == d.FP16 else d.STATE_FP32
     with d.Classifier(sequence=g, level_table=tab, precision=precision, device=device,
-                      serve_batches=batches) as clf:
+                      serve_batches=batches, state_precision=state_precision) as clf:
         accept, reject = readuntil.calibrate(clf, reads, cfg)
         rec = readuntil.run(clf, reads, cfg, accept, reject, state_budget_bytes=spec["budget_gb"] * 1e9)
     rec["workload"] = (f"{name}: {spec['channels']} channels, 1,600-sample chunks every 0.4 s, Poisson read "
                        f"starts 1/s/channel, <= 3 chunks per decision, {spec['genome_len'] // 1_000_000} Mb "
                        f"seeded genome ({2 * (spec['genome_len'] - 5)} columns), row-state budget "
-                       f"{spec['budget_gb']:.0f} GB")
+                       f"{spec['budget_gb']:.0f} GB, {'FP16' if state_precision == d.STATE_FP16 else 'FP32'} "
+                       f"row state")
     return rec
 
 
@@ -421,7 +424,8 @@ def run_ours(args, rank, world, local):
                   "other_score_per_sample_min": float((res["score"] / res["n_samples"])[~t_mask].min())},
     }
     if args.serving != "none" and rank == 0:
-        line["serving"] = run_serving(args.serving, precision, local, args.serving_seconds, args.serve_batches)
+        line["serving"] = run_serving(args.serving, precision, local, args.serving_seconds, args.serve_batches,
+                                      args.state)
     if args.reads:
         line["config"]["workload"] += f" (first {n_reads} reads only)"
     if rank == 0:
@@ -443,6 +447,8 @@ def main():
     ap.add_argument("--skip-ref-gpu", action="store_true",
                     help="reference arm: do not time the reference's own GPU kernel beside the CPU line")
     ap.add_argument("--precision", choices=["fp16", "fp32", "mixed"], default="fp16")
+    ap.add_argument("--state", choices=["fp32", "fp16"], default="fp32",
+                    help="serving row state: FP32 values or FP16 cells with frame offsets (FP16 cells only)")
     ap.add_argument("--recurrence", choices=["no_ref_del", "ref_del"], default="no_ref_del",
                     help="ref_del: the left predecessor of DTW.cu:23-29 (FP32 cells)")
     ap.add_argument("--reads", type=int, default=0,

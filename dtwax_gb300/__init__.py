@@ -28,6 +28,7 @@ STATUS = {0: "OK", -1: "E_ARG", -2: "E_IO", -3: "E_FORMAT", -4: "E_CUDA", -5: "E
           -6: "E_TIMEOUT", -7: "E_CAPACITY", -8: "E_STATE"}
 FP16, FP32, MIXED = 0, 1, 2  # MIXED: FP16 differences, FP32 path cost
 NO_REF_DEL, REF_DEL = 0, 1     # recurrence: without / with the left predecessor
+STATE_FP32, STATE_FP16 = 0, 1  # serving row state
 STRANDS_PAIRED, STRANDS_CONCAT = 0, 1
 ABI_VERSION = 2
 
@@ -48,7 +49,7 @@ class Config(ctypes.Structure):
         ("max_batch_reads", ctypes.c_int32), ("cells_per_thread", ctypes.c_int32),
         ("chunk_strips", ctypes.c_int32), ("warps_per_cta", ctypes.c_int32),
         ("use_graphs", ctypes.c_int32), ("serve_batches", ctypes.c_int32), ("recurrence", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("state_precision", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4),
     ]
 
 

@@ -220,6 +220,17 @@ int choose_chunk_strips(int64_t strips_per_read, int64_t n_tasks, double mean_ro
   return best_g;
 }
 
+// Serving row state kept as FP16 cells plus frame offsets (FP16 handles only).
+bool state_fp16(const dtwx_handle *h) {
+  return h->cfg.state_precision == DTWX_STATE_FP16 && h->cfg.precision == DTWX_FP16;
+}
+
+// Floats of row state per read slot: FP32 fwd and rev planes, or half2 cells
+// (one float each) then a float2 offset per 512-column group.
+int64_t state_slot_floats(const dtwx_handle *h) {
+  return state_fp16(h) ? h->m_pad + 2 * (h->m_pad / 512) : 2 * h->m_pad;
+}
+
 // Reference buffer a sweep of this precision reads when TMA is off.
 const void *ref_for(const dtwx_handle *h, int precision) {
   return precision == 0 ? h->ref16.p : (precision == 2 ? h->ref16p.p : h->ref32.p);
@@ -322,6 +333,7 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
     p.ref_layout = 1;
     p.strands = strands;
     p.ref_del = h->cfg.recurrence == DTWX_REF_DEL ? 1 : 0;
+    p.state_fp16 = state_fp16(h) ? 1 : 0;
     const int ii = inst_index(precision, sh.S);
     p.use_tma = h->tmap_ok[precision][ii] ? 1 : 0;
     // inside a stream capture the timing events become event-record nodes
@@ -646,6 +658,10 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
     return fail(nullptr, DTWX_E_ARG, "bad strand_mode");
   if (cfg.recurrence != DTWX_NO_REF_DEL && cfg.recurrence != DTWX_REF_DEL)
     return fail(nullptr, DTWX_E_ARG, "bad recurrence");
+  if (cfg.state_precision != DTWX_STATE_FP32 && cfg.state_precision != DTWX_STATE_FP16)
+    return fail(nullptr, DTWX_E_ARG, "bad state_precision");
+  if (cfg.state_precision == DTWX_STATE_FP16 && cfg.precision != DTWX_FP16)
+    return fail(nullptr, DTWX_E_ARG, "FP16 row state needs DTWX_FP16 cells");
   if (cfg.recurrence == DTWX_REF_DEL && cfg.precision != DTWX_FP32)
     return fail(nullptr, DTWX_E_ARG, "the REF_DEL recurrence is built for FP32 cells");
   if (cfg.cells_per_thread &&
@@ -1081,7 +1097,7 @@ int dtwx_serve_start(dtwx_handle *h, int32_t max_in_flight, double state_budget_
   if (h->serving) return fail(h, DTWX_E_STATE, "serving already started");
   if (chunks_per_decision <= 0) return fail(h, DTWX_E_ARG, "chunks_per_decision must be > 0");
   CK(h, cudaSetDevice(h->device));
-  const double slot_bytes = 2.0 * (double)h->m_pad * sizeof(float);  // fwd and rev planes
+  const double slot_bytes = (double)state_slot_floats(h) * sizeof(float);
   int64_t slots = max_in_flight > 0 ? max_in_flight : 0;
   if (slots == 0 && state_budget_bytes <= 0) {
     // neither given: the row-state pool may take half of the free device memory
@@ -1296,7 +1312,7 @@ int dtwx_serve_step(dtwx_handle *h) {
     t.q_off = off;
     t.n = batch[i].n;
     t.flags = kTaskSaveState | (r.chunks_done > 0 ? kTaskResume : 0);
-    t.state_off = (int64_t)r.slot * 2 * h->m_pad;
+    t.state_off = (int64_t)r.slot * state_slot_floats(h);
     t.out_slot = i;
     nsamp[i] = batch[i].n;
     src_off[i] = off;

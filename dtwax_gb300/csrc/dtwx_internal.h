@@ -43,7 +43,7 @@ struct SdtwParams {
   const int32_t *order;        // processing order of tasks (longest first); NULL = identity
   unsigned long long *keys;    // 2 per out slot: (orderable score << 32) | end column
   float *state;                // row-state pool (absolute FP32 values, per read a fwd and a rev
-                               // plane of m_pad floats), NULL if unused
+                               // plane of m_pad floats; or the FP16 layout of state_fp16), NULL if unused
   char *seam;                  // per-warp scratch (seam columns + epoch offsets)
   int32_t *counter;            // work-queue ticket counter (zeroed before launch)
   int32_t *err;                // device error flags
@@ -61,6 +61,8 @@ struct SdtwParams {
                                // MIXED is always planar FP16
   int32_t strands;             // FP32/MIXED strands per task: 2 (paired), 1 (concatenated sequence); 0 = 2
   int32_t ref_del;             // 1: REF_DEL recurrence (left predecessor); needs one chunk per task
+  int32_t state_fp16;          // FP16 cells: row state as half2 cells (m_pad) then one float2
+                               // frame offset per 512-column group (m_pad / 512)
 };
 
 // Per-warp scratch layout, in bytes, for cells of `pair_bytes` bytes.

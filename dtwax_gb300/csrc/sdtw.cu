@@ -405,14 +405,16 @@ __device__ __forceinline__ void row(typename Pol<PREC>::V (&D)[S],
 // Register cap per instance: the S cells and S reference elements of a lane
 // plus about 40 registers of bookkeeping (70 for the REF_DEL scan), rounded to
 // 128 or 168 (16 or 12 warps/SM).
-template <int S, int PREC, bool RD>
+template <int S, int PREC, bool RD, bool ST16 = false>
 constexpr int sdtw_reg_cap() { return S + S * Pol<PREC>::RB / 4 + (RD ? 70 : 40) <= 128 ? 128 : 168; }
 
 // RD: the REF_DEL recurrence (FP32 cells).  A horizontal run can cross any
 // column chunk, so the host gives REF_DEL tasks one chunk (no halo).
-template <int S, int PREC, bool RD>
-__global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD>())) sdtw_kernel(const __grid_constant__ CUtensorMap tmap,
-                                                                        const SdtwParams p) {
+// ST16: FP16 cells whose serving row state is FP16 (p.state_fp16); a separate
+// instance, so the other instances carry none of its registers.
+template <int S, int PREC, bool RD, bool ST16>
+__global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
+    const __grid_constant__ CUtensorMap tmap, const SdtwParams p) {
   using P = Pol<PREC>;
   using V = typename P::V;
   using RV = typename P::RV;
@@ -426,6 +428,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD>())) sdtw_kernel(const __g
   static_assert(STRIP_BYTES % 1024 == 0, "strip tile must keep 1024-byte alignment");
   static_assert(S % 8 == 0, "row state and reference move in 16-byte groups");
   static_assert(!RD || PREC == 1, "the REF_DEL row is built for FP32 cells");
+  static_assert(!ST16 || PREC == 0, "the FP16 row state is built for FP16 cells");
 
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
@@ -518,6 +521,41 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD>())) sdtw_kernel(const __g
       if (resume) {
         const int64_t c0 = x + (int64_t)lane * S;
         if constexpr (PREC == 0) {
+          if constexpr (ST16) {
+            // FP16 row state: half2 cells relative to the offset of their
+            // 512-column group (the saving strip's frame); re-based onto this
+            // strip's minimum
+            const uint4 *hc = reinterpret_cast<const uint4 *>(reinterpret_cast<const __half2 *>(st_plane0) + c0);
+            const float2 *og = reinterpret_cast<const float2 *>(st_plane0 + p.m_pad);
+#pragma unroll
+            for (int k = 0; k < S / 4; ++k) {
+              const uint4 u = hc[k];
+              D[4 * k] = bits_as<__half2>(u.x);
+              D[4 * k + 1] = bits_as<__half2>(u.y);
+              D[4 * k + 2] = bits_as<__half2>(u.z);
+              D[4 * k + 3] = bits_as<__half2>(u.w);
+            }
+            float mx = __int_as_float(0x7f800000), my = mx;
+#pragma unroll
+            for (int k = 0; k < S; ++k) {
+              const float2 o = og[(c0 + k) >> 9];
+              const float2 v = __half22float2(D[k]);
+              mx = fminf(mx, v.x + o.x);
+              my = fminf(my, v.y + o.y);
+            }
+#pragma unroll
+            for (int m = 16; m >= 1; m >>= 1) {
+              mx = fminf(mx, __shfl_xor_sync(FULL_MASK, mx, m));
+              my = fminf(my, __shfl_xor_sync(FULL_MASK, my, m));
+            }
+            O = make_float2(mx, my);
+#pragma unroll
+            for (int k = 0; k < S; ++k) {
+              const float2 o = og[(c0 + k) >> 9];
+              const float2 v = __half22float2(D[k]);
+              D[k] = __floats2half2_rn(v.x + o.x - mx, v.y + o.y - my);
+            }
+          } else {
           // two passes over the saved planes: strip minimum first, then the cells
           const float4 *f0 = reinterpret_cast<const float4 *>(st_plane0 + c0);
           const float4 *f1 = reinterpret_cast<const float4 *>(st_plane0 + p.m_pad + c0);
@@ -541,6 +579,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD>())) sdtw_kernel(const __g
             D[4 * k + 1] = __floats2half2_rn(u.y - mx, v.y - my);
             D[4 * k + 2] = __floats2half2_rn(u.z - mx, v.z - my);
             D[4 * k + 3] = __floats2half2_rn(u.w - mx, v.w - my);
+          }
           }
         } else {
           const float4 *f = reinterpret_cast<const float4 *>(st_plane0 + (int64_t)strand * p.m_pad + c0);
@@ -683,6 +722,17 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD>())) sdtw_kernel(const __g
       if (relevant) {
         const int64_t c0 = x + (int64_t)lane * S;
         if constexpr (PREC == 0) {
+          if (ST16 && save) {
+            // half2 cells in this strip's frame, the frame offset once per 512-column group
+            uint4 *hc = reinterpret_cast<uint4 *>(reinterpret_cast<__half2 *>(p.state + t.state_off) + c0);
+#pragma unroll
+            for (int k = 0; k < S / 4; ++k)
+              hc[k] = make_uint4(cell_bits<0>(D[4 * k]), cell_bits<0>(D[4 * k + 1]), cell_bits<0>(D[4 * k + 2]),
+                                 cell_bits<0>(D[4 * k + 3]));
+            float2 *og = reinterpret_cast<float2 *>(p.state + t.state_off + p.m_pad);
+            og[c0 >> 9] = O;  // every lane of the strip stores the same value
+            og[(c0 + S - 1) >> 9] = O;
+          }
 #pragma unroll
           for (int k = 0; k < S; ++k) {
             const float2 v = __half22float2(D[k]);
@@ -693,7 +743,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD>())) sdtw_kernel(const __g
               if (vy < besty) { besty = vy; coly = col; }
             }
           }
-          if (save) {
+          if (!ST16 && save) {
             float4 *f0 = reinterpret_cast<float4 *>(p.state + t.state_off + c0);
             float4 *f1 = reinterpret_cast<float4 *>(p.state + t.state_off + p.m_pad + c0);
 #pragma unroll
@@ -735,11 +785,11 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD>())) sdtw_kernel(const __g
 
 // ---------------------------------------------------------------- instances / launch
 
-template <int S, int PREC, bool RD = false>
+template <int S, int PREC, bool RD = false, bool ST16 = false>
 static cudaError_t launch_inst(int warps, int grid, const SdtwParams &p, const CUtensorMap *tmap,
                                cudaStream_t s) {
   const size_t smem = sdtw_smem_bytes(PREC, S, warps);
-  auto fn = sdtw_kernel<S, PREC, RD>;
+  auto fn = sdtw_kernel<S, PREC, RD, ST16>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   CUtensorMap dummy;
@@ -751,11 +801,11 @@ static cudaError_t launch_inst(int warps, int grid, const SdtwParams &p, const C
   return cudaGetLastError();
 }
 
-template <int S, int PREC, bool RD = false>
+template <int S, int PREC, bool RD = false, bool ST16 = false>
 static int occ_inst(int warps) {
   int n = 0;
   const size_t smem = sdtw_smem_bytes(PREC, S, warps);
-  auto fn = sdtw_kernel<S, PREC, RD>;
+  auto fn = sdtw_kernel<S, PREC, RD, ST16>;
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, warps * kWarp, smem) != cudaSuccess) return 0;
@@ -782,12 +832,19 @@ bool sdtw_instance_exists(int precision, int S, bool ref_del) {
   if (precision == PREC && cells_per_thread == S) return CALL<S, PREC>
 #define DTWX_DISPATCH_RD(S, CALL) \
   if (precision == 1 && cells_per_thread == S) return CALL<S, 1, true>
+#define DTWX_DISPATCH_ST16(S, CALL) \
+  if (precision == 0 && cells_per_thread == S) return CALL<S, 0, false, true>
 
 cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, int grid,
                         const SdtwParams &p, const CUtensorMap *tmap, cudaStream_t s) {
   if (p.ref_del) {
     DTWX_DISPATCH_RD(16, launch_inst)(warps_per_cta, grid, p, tmap, s);
     DTWX_DISPATCH_RD(32, launch_inst)(warps_per_cta, grid, p, tmap, s);
+    return cudaErrorInvalidValue;
+  }
+  if (p.state_fp16) {
+    DTWX_DISPATCH_ST16(32, launch_inst)(warps_per_cta, grid, p, tmap, s);
+    DTWX_DISPATCH_ST16(48, launch_inst)(warps_per_cta, grid, p, tmap, s);
     return cudaErrorInvalidValue;
   }
   DTWX_DISPATCH(0, 32, launch_inst)(warps_per_cta, grid, p, tmap, s);

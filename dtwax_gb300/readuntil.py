@@ -152,10 +152,13 @@ def _loop(clf, seq, cfg: ServeConfig, drain: bool) -> dict:
     decided_in_window = 0
     chunks_in_window = 0
     end_s = cfg.warmup_s + cfg.duration_s
+    st0 = None
     while True:
         now_s = (now_ms() - t_base) / 1e3
         if now_s >= end_s:
             break
+        if st0 is None and now_s >= cfg.warmup_s:
+            st0 = clf.stats()
         for (t, ch, rn, x, last) in seq.due(now_s):
             clf.submit_chunk(ch, rn, x, is_last=last, arrival_ms=t_base + t * 1e3)
             if t >= cfg.warmup_s:
@@ -183,6 +186,8 @@ def _loop(clf, seq, cfg: ServeConfig, drain: bool) -> dict:
         "channels": cfg.channels, "chunk_samples": cfg.chunk, "duration_s": cfg.duration_s,
         "reads_per_s": decided_in_window / cfg.duration_s,
         "chunks_per_s": chunks_in_window / cfg.duration_s,
+        # chunk-steps the GPU aligned per second in the window (offered load is chunks_per_s)
+        "chunks_processed_per_s": (st["chunks_processed"] - (st0 or st)["chunks_processed"]) / cfg.duration_s,
         "p50_latency_ms": float(np.percentile(lat, 50)) if lat.size else None,
         "p99_latency_ms": float(np.percentile(lat, 99)) if lat.size else None,
         "max_latency_ms": float(lat.max()) if lat.size else None,

@@ -50,6 +50,11 @@ extern "C" {
                              FP32 cells only; a read is one work item per strand (a
                              horizontal run can cross any column chunk) */
 
+/* serving row state (the last DP row of a read between its chunks) */
+#define DTWX_STATE_FP32 0 /* absolute FP32 values: 8 bytes per column pair */
+#define DTWX_STATE_FP16 1 /* DTWX_FP16 cells only: half2 cells relative to a float2 frame offset per
+                             512 columns, about 4 bytes per column pair (twice the reads per budget) */
+
 /* how the two strands are scored */
 #define DTWX_STRANDS_PAIRED 0 /* fwd and rev aligned separately (DTW.cu half2 .x/.y) */
 #define DTWX_STRANDS_CONCAT 1 /* one sequence fwd||rev (load_reference.hpp:36-37, sdtw.py:234) */
@@ -79,7 +84,8 @@ typedef struct dtwx_config {
                               directly, the second is captured, later ones are replays */
   int32_t serve_batches;   /* serving batches in flight at once (1..4), 0 = 2 */
   int32_t recurrence;      /* DTWX_NO_REF_DEL (default) or DTWX_REF_DEL */
-  int32_t reserved[5];
+  int32_t state_precision; /* DTWX_STATE_FP32 (default) or DTWX_STATE_FP16 */
+  int32_t reserved[4];
 } dtwx_config;
 
 /* Per-read outcome.  end_pos is the DP column (0-based k-mer position on the

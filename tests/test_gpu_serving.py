@@ -85,6 +85,39 @@ def test_resume_matches_oracle(setup, oracle, precision, rtol):
                 assert (d["end_pos"], d["strand"]) == (e, st)
 
 
+def test_resume_fp16_state_matches_oracle(setup, oracle):
+    """FP16 row state (half2 cells + a frame offset per 512 columns) resumed
+    chunk by chunk; a batch shape that differs between chunks (autotuned
+    buckets) re-bases the saved frames."""
+    import dtwax_gb300 as d
+    g, o, tab, reads = setup
+    for cells in (32, 48):
+        with make_classifier(g, tab, precision=d.FP16, state_precision=d.STATE_FP16, threshold=-1.0,
+                             cells_per_thread=cells) as clf:
+            fwd, rev = clf.reference()
+            chunks = {i: split(reads.read(i), 1600) for i in range(reads.n)}
+            got = serve_reads(clf, chunks, chunks_per_decision=3)
+        for i in range(reads.n):
+            want = oracle_decisions(oracle, fwd.astype(np.float64), rev.astype(np.float64), chunks[i][:3])
+            for dd, (s, e, st) in zip(got[i], want):
+                assert dd["score"] == pytest.approx(s, rel=1e-2)
+
+
+def test_fp16_state_halves_the_row_bytes(setup):
+    import dtwax_gb300 as d
+    g, o, tab, reads = setup
+    budget = 64 * 8 * (40_000 + 6144.0)  # 64 reads of FP32 rows
+    with make_classifier(g, tab, precision=d.FP16) as clf:
+        clf.serve_start(state_budget_bytes=budget)
+        n32 = clf.stats()["max_in_flight"]
+    with make_classifier(g, tab, precision=d.FP16, state_precision=d.STATE_FP16) as clf:
+        clf.serve_start(state_budget_bytes=budget)
+        n16 = clf.stats()["max_in_flight"]
+    assert n16 >= 2 * n32 - 2 and n32 >= 60
+    with pytest.raises(d.DtwxError):
+        make_classifier(g, tab, precision=d.FP32, state_precision=d.STATE_FP16)
+
+
 def test_resume_ref_del_matches_oracle(setup, oracle):
     """The REF_DEL recurrence resumed chunk by chunk from the saved rows."""
     import dtwax_gb300 as d

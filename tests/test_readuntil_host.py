@@ -43,6 +43,7 @@ class FakeServer:
 
     def stats(self):
         return {"mean_batch_reads": 1.0, "batches": self.steps, "mean_batch_ms": 0.0, "max_batch_ms": 0.0,
+                "chunks_processed": self.submitted,
                 "reads_deferred": 0, "max_in_flight": 0, "queue_depth": 0, "state_bytes": 0.0}
 
 
