@@ -42,6 +42,23 @@ def test_config_default(built_lib):
     assert ctypes.sizeof(d.Config) == 96  # same static_assert in api.cpp
 
 
+def test_config_combinations_are_checked(built_lib, kat, tmp_path):
+    """Invalid precision / recurrence / row-state combinations are refused
+    before any device work (code -1, DTWX_E_ARG), with or without a GPU."""
+    import dtwax_gb300 as d
+    fasta, model = write_kat_files(kat, str(tmp_path))
+    c = d.default_config()
+    assert c.recurrence == d.NO_REF_DEL and c.state_precision == d.STATE_FP32
+    bad = [dict(precision=3), dict(recurrence=2), dict(state_precision=2),
+           dict(precision=d.FP16, recurrence=d.REF_DEL), dict(precision=d.MIXED, recurrence=d.REF_DEL),
+           dict(precision=d.FP32, state_precision=d.STATE_FP16),
+           dict(precision=d.FP32, recurrence=d.REF_DEL, cells_per_thread=48)]
+    for kw in bad:
+        with pytest.raises(d.DtwxError) as e:
+            d.Classifier(fasta=fasta, kmer_model=model, **kw)
+        assert e.value.code == -1, kw
+
+
 def test_create_without_gpu_fails_loudly(built_lib, tmp_path, kat):
     """No CPU fallback: on a machine without a GPU creation must fail."""
     import dtwax_gb300 as d
