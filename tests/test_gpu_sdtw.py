@@ -197,6 +197,27 @@ def test_fp16_chunking_within_tolerance(lib, oracle, genome_pair, cells, strips)
     np.testing.assert_allclose(res["score_rev"], sr, rtol=FP16_RTOL)
 
 
+@pytest.mark.parametrize("precision", [1, 0])
+def test_long_and_short_reads_in_one_batch(lib, oracle, genome_pair, precision):
+    """Reads far longer than the reference window (40,000 and 12,345 samples)
+    next to tiny ones: the seam buffers are sized by the longest read, halo
+    strips of short reads stop early, and every read matches the oracle."""
+    g, o = genome_pair
+    tab = synth.level_table()
+    lengths = [40_000, 3, 12_345, 1, 700]
+    reads = reads_of_lengths(g, o, tab, lengths)
+    with make_classifier(g, tab, precision=precision) as clf:
+        res = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        ora = oracle_classify(oracle, clf, reads.raw, reads.offsets)
+    assert (res["n_samples"] == np.array(lengths)).all()
+    if precision == 1:
+        check_fp32(res, ora)
+    else:
+        sf, ef, sr, er = ora
+        np.testing.assert_allclose(res["score_fwd"], sf, rtol=FP16_RTOL, atol=1e-2)
+        np.testing.assert_allclose(res["score_rev"], sr, rtol=FP16_RTOL, atol=1e-2)
+
+
 def test_edge_cases(lib, oracle):
     import dtwax_gb300 as d
     tab = synth.level_table()
