@@ -322,8 +322,8 @@ def run_ours(args, rank, world, local):
 
     precision = {"fp16": d.FP16, "fp32": d.FP32, "mixed": d.MIXED}[args.precision]
     ref_del = args.recurrence == "ref_del"
-    if ref_del and precision != d.FP32:
-        raise SystemExit("--recurrence ref_del runs FP32 cells (--precision fp32)")
+    if ref_del and precision == d.MIXED:
+        raise SystemExit("--recurrence ref_del runs FP16 or FP32 cells")
     w = synth.make_workload(args.workload, n_reads=args.reads or None)
     cells = w.cells()
     n_reads = w.reads.n
@@ -405,7 +405,9 @@ def run_ours(args, rank, world, local):
     mhz = clock_rec.get("sm_mhz") or 2070.0
     per_sm_cycle = {d.FP16: 64.0, d.FP32: 128.0 / 3.0, d.MIXED: 128.0 / 2.5}[precision]
     if ref_del:
-        per_sm_cycle = 128.0 / 9.0  # REF_DEL: 6 + 3 issue slots per cell in the two row passes
+        # REF_DEL: FP32 cells take 6 + 3 issue slots per cell in the two row passes;
+        # FP16 pairs take 6 FMA-pipe instructions (2 cycles each) per pair
+        per_sm_cycle = 128.0 / 9.0 if precision == d.FP32 else 64.0 / 3.0
     theoretical = sms * per_sm_cycle * mhz * 1e6 / 1e9
     traffic = traffic_from_profile(args.precision)
     t_mask = w.reads.target == 1
@@ -463,7 +465,7 @@ def main():
     ap.add_argument("--state", choices=["fp32", "fp16"], default="fp32",
                     help="serving row state: FP32 values or FP16 cells with frame offsets (FP16 cells only)")
     ap.add_argument("--recurrence", choices=["no_ref_del", "ref_del"], default="no_ref_del",
-                    help="ref_del: the left predecessor of DTW.cu:23-29 (FP32 cells)")
+                    help="ref_del: the left predecessor of DTW.cu:23-29 (FP16 or FP32 cells)")
     ap.add_argument("--reads", type=int, default=0,
                     help="use only the first N reads of the workload (small cases for profiling)")
     ap.add_argument("--skip-cpu", action="store_true", help="do not time the CPU baseline")

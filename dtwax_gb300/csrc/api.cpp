@@ -250,7 +250,7 @@ Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_row
   const bool use_t = t != h->tuned.end();
   // defaults measured on the 1 Mb / 2,048-read batch: 48 cells per lane (64 for
   // MIXED, whose reference takes half the registers) in 4-warp CTAs; the REF_DEL
-  // instances have 16 or 32 cells per lane
+  // instances have 32 cells per lane (and 16 in FP32)
   const bool rd = h->cfg.recurrence == DTWX_REF_DEL;
   const int def_S = rd ? 32 : (precision == 2 ? 64 : 48);
   s.S = o.S ? o.S : (f.S ? f.S : (use_t ? t->second.S : def_S));
@@ -662,8 +662,10 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
     return fail(nullptr, DTWX_E_ARG, "bad state_precision");
   if (cfg.state_precision == DTWX_STATE_FP16 && cfg.precision != DTWX_FP16)
     return fail(nullptr, DTWX_E_ARG, "FP16 row state needs DTWX_FP16 cells");
-  if (cfg.recurrence == DTWX_REF_DEL && cfg.precision != DTWX_FP32)
-    return fail(nullptr, DTWX_E_ARG, "the REF_DEL recurrence is built for FP32 cells");
+  if (cfg.recurrence == DTWX_REF_DEL && cfg.precision == DTWX_MIXED)
+    return fail(nullptr, DTWX_E_ARG, "the REF_DEL recurrence is built for FP16 and FP32 cells");
+  if (cfg.recurrence == DTWX_REF_DEL && cfg.state_precision == DTWX_STATE_FP16)
+    return fail(nullptr, DTWX_E_ARG, "REF_DEL keeps an FP32 row state");
   if (cfg.cells_per_thread &&
       !sdtw_instance_exists(cfg.precision, cfg.cells_per_thread, cfg.recurrence == DTWX_REF_DEL))
     return fail(nullptr, DTWX_E_ARG, "cells_per_thread has no compiled kernel for this precision");

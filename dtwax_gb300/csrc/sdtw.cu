@@ -323,52 +323,93 @@ __device__ __forceinline__ void sweep_row_mixed(float (&D)[S], const __half2 (&R
   }
 }
 
-// The REF_DEL row (FP32 cells): the cell to the left in the same row is a
-// third predecessor, D[j] = min(v[j], c[j] + D[j-1]) with c = d^2 and
+// The REF_DEL row: the cell to the left in the same row is a third
+// predecessor, D[j] = min(v[j], c[j] + D[j-1]) with c = d^2 and
 // v = c + min(up, diag).  That is a scan along the row in the (min, +)
 // semiring, done in three passes:
 //  1. each lane runs its S columns with +inf entering on the left, keeping the
 //     local values P[j] in D and the lane's map x -> min(P[S-1], x + sum c);
-//  2. the 32 maps are composed by a warp scan, (a1, b1) then (a2, b2) being
-//     (a1 + a2, min(b2, b1 + a2)), which gives each lane its left input X;
-//  3. D[j] = min(P[j], X + c[0] + ... + c[j]).
+//     the S columns are two halves run as two independent chains (twice the
+//     instruction-level parallelism), whose maps are then composed;
+//  2. the 32 lane maps are composed by a warp scan, (a1, b1) then (a2, b2)
+//     being (a1 + a2, min(b2, b1 + a2)), which gives each lane its left input;
+//  3. D[j] = min(P[j], X + c[0] + ... + c[j]), again as two chains.
 // seam_diag / seam_left are the left strip's last column on the previous and
-// on this row (lane 0 only).
-template <int S>
-__device__ __forceinline__ void sweep_row_refdel(float (&D)[S], const float (&R)[S], float q, float seam_diag,
-                                                 float seam_left, uint32_t m0, int lane) {
-  const float up = __shfl_up_sync(FULL_MASK, D[S - 1], 1);
-  float dprev = __uint_as_float((__float_as_uint(up) & ~m0) | (__float_as_uint(seam_diag) & m0));
-  float pacc = __int_as_float(0x7f800000), a = 0.f;
+// on this row (lane 0 only).  RdOps is the arithmetic of the cell type.
+template <typename V>
+struct RdOps;
+template <>
+struct RdOps<float> {
+  __device__ __forceinline__ static float sub(float a, float b) { return a - b; }
+  __device__ __forceinline__ static float add(float a, float b) { return a + b; }
+  __device__ __forceinline__ static float fma(float a, float b, float c) { return fmaf(a, b, c); }
+  __device__ __forceinline__ static float vmin(float a, float b) { return fminf(a, b); }
+  __device__ __forceinline__ static float inf() { return __int_as_float(0x7f800000); }
+  __device__ __forceinline__ static float zero() { return 0.f; }
+  __device__ __forceinline__ static uint32_t bits(float v) { return __float_as_uint(v); }
+};
+template <>
+struct RdOps<__half2> {
+  // FP16 pairs in the strip's running-minimum frame; cost sums that overflow
+  // half become +inf, which only drops left-boundary paths far above every
+  // cell of the row
+  __device__ __forceinline__ static __half2 sub(__half2 a, __half2 b) { return __hsub2(a, b); }
+  __device__ __forceinline__ static __half2 add(__half2 a, __half2 b) { return __hadd2(a, b); }
+  __device__ __forceinline__ static __half2 fma(__half2 a, __half2 b, __half2 c) { return __hfma2(a, b, c); }
+  __device__ __forceinline__ static __half2 vmin(__half2 a, __half2 b) { return __hmin2(a, b); }
+  __device__ __forceinline__ static __half2 inf() { return Pol<0>::inf(); }
+  __device__ __forceinline__ static __half2 zero() { return Pol<0>::zero(); }
+  __device__ __forceinline__ static uint32_t bits(__half2 v) { return cell_bits<0>(v); }
+};
+
+template <int S, typename V>
+__device__ __forceinline__ void sweep_row_refdel(V (&D)[S], const V (&R)[S], V q, V seam_diag, V seam_left,
+                                                 uint32_t m0, int lane) {
+  using O = RdOps<V>;
+  constexpr int H = S / 2;
+  const V up = __shfl_up_sync(FULL_MASK, D[S - 1], 1);
+  V dp0 = bits_as<V>((O::bits(up) & ~m0) | (O::bits(seam_diag) & m0));
+  V dp1 = D[H - 1];  // the previous row's value left of the second half
+  V p0 = O::inf(), p1 = O::inf(), a0 = O::zero(), a1 = O::zero();
 #pragma unroll
-  for (int k = 0; k < S; ++k) {
-    const float top = D[k];
-    const float d = R[k] - q;
-    const float v = fmaf(d, d, fminf(top, dprev));
-    dprev = top;
-    pacc = fminf(v, fmaf(d, d, pacc));
-    a = fmaf(d, d, a);
-    D[k] = pacc;
+  for (int k = 0; k < H; ++k) {
+    const V t0 = D[k], t1 = D[H + k];
+    const V d0 = O::sub(R[k], q), d1 = O::sub(R[H + k], q);
+    const V v0 = O::fma(d0, d0, O::vmin(t0, dp0));
+    const V v1 = O::fma(d1, d1, O::vmin(t1, dp1));
+    dp0 = t0;
+    dp1 = t1;
+    p0 = O::vmin(v0, O::fma(d0, d0, p0));
+    p1 = O::vmin(v1, O::fma(d1, d1, p1));
+    a0 = O::fma(d0, d0, a0);
+    a1 = O::fma(d1, d1, a1);
+    D[k] = p0;
+    D[H + k] = p1;
   }
-  float b = pacc;
+  // the lane's map: the first half's map, then the second half's
+  V a = O::add(a0, a1);
+  V b = O::vmin(p1, O::add(p0, a1));
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
-    const float ua = __shfl_up_sync(FULL_MASK, a, off);
-    const float ub = __shfl_up_sync(FULL_MASK, b, off);
+    const V ua = __shfl_up_sync(FULL_MASK, a, off);
+    const V ub = __shfl_up_sync(FULL_MASK, b, off);
     const bool act = lane >= off;
-    b = act ? fminf(b, ub + a) : b;
-    a = act ? ua + a : a;
+    b = act ? O::vmin(b, O::add(ub, a)) : b;
+    a = act ? O::add(ua, a) : a;
   }
   // exclusive prefix: the composed map of lanes 0..l-1 applied to seam_left
-  const float ea = __shfl_up_sync(FULL_MASK, a, 1);
-  const float eb = __shfl_up_sync(FULL_MASK, b, 1);
-  const float xin = fminf(eb, seam_left + ea);
-  float x = __uint_as_float((__float_as_uint(xin) & ~m0) | (__float_as_uint(seam_left) & m0));
+  const V ea = __shfl_up_sync(FULL_MASK, a, 1);
+  const V eb = __shfl_up_sync(FULL_MASK, b, 1);
+  const V xin = O::vmin(eb, O::add(seam_left, ea));
+  V x0 = bits_as<V>((O::bits(xin) & ~m0) | (O::bits(seam_left) & m0));
+  V x1 = O::vmin(p0, O::add(x0, a0));  // the true value left of the second half
 #pragma unroll
-  for (int k = 0; k < S; ++k) {
-    const float d = R[k] - q;
-    x = fmaf(d, d, x);
-    D[k] = fminf(D[k], x);
+  for (int k = 0; k < H; ++k) {
+    const V d0 = O::sub(R[k], q), d1 = O::sub(R[H + k], q);
+    x0 = O::fma(d0, d0, x0);
+    x1 = O::fma(d1, d1, x1);
+    D[k] = O::vmin(D[k], x0);
+    D[H + k] = O::vmin(D[H + k], x1);
   }
 }
 
@@ -390,6 +431,14 @@ __device__ __forceinline__ unsigned long long make_key(float v, int64_t j) {
 }
 
 // ---------------------------------------------------------------- the persistent kernel
+
+// One REF_DEL row for the policy.
+template <int S, int PREC>
+__device__ __forceinline__ void row_refdel(typename Pol<PREC>::V (&D)[S], const typename Pol<PREC>::RV (&R)[S],
+                                           typename Pol<PREC>::QW qq, typename Pol<PREC>::V seam_diag,
+                                           typename Pol<PREC>::V seam_left, uint32_t m0, int lane) {
+  sweep_row_refdel<S, typename Pol<PREC>::V>(D, R, qq, seam_diag, seam_left, m0, lane);
+}
 
 // One DP row for the policy: FP16 pairs and FP32 share sweep_row, MIXED has its own.
 template <int S, int PREC>
@@ -427,7 +476,8 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
   constexpr int K = kRescaleRows;
   static_assert(STRIP_BYTES % 1024 == 0, "strip tile must keep 1024-byte alignment");
   static_assert(S % 8 == 0, "row state and reference move in 16-byte groups");
-  static_assert(!RD || PREC == 1, "the REF_DEL row is built for FP32 cells");
+  static_assert(!RD || PREC <= 1, "the REF_DEL row is built for FP16 pairs and FP32 cells");
+  static_assert(!(RD && ST16), "REF_DEL with the FP16 row state is not built");
   static_assert(!ST16 || PREC == 0, "the FP16 row state is built for FP16 cells");
 
   extern __shared__ unsigned char smem_raw[];
@@ -662,12 +712,19 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
         V sout = vinf;
         // REF_DEL: lane l of lwin holds the left strip's value on row i0+l itself
         V lwin = vinf;
-        if constexpr (RD) lwin = P::sel(lane == kWarp - 1, P::shfl(sn, 0), __shfl_down_sync(FULL_MASK, swin, 1));
+        if constexpr (RD) {
+          V last = P::shfl(sn, 0);  // the left strip's value on row i0+31, stored after its rescale
+          if constexpr (PREC == 0) {
+            // that value is in the left strip's next frame: re-base with the next epoch's offset
+            last = __hadd2(last, __float22half2_rn(make_float2(off_next.x - O.x, off_next.y - O.y)));
+          }
+          lwin = P::sel(lane == kWarp - 1, last, __shfl_down_sync(FULL_MASK, swin, 1));
+        }
         if (rows - i0 >= kWarp) {
 #pragma unroll 4
           for (int il = 0; il < kWarp; ++il) {
             if constexpr (RD)
-              sweep_row_refdel<S>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
+              row_refdel<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
             else
               row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
             sout = P::sel(lane == il, P::shfl(D[S - 1], 31), sout);
@@ -697,7 +754,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
           const int cnt = rows - i0;
           for (int il = 0; il < cnt; ++il) {
             if constexpr (RD)
-              sweep_row_refdel<S>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
+              row_refdel<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
             else
               row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
             sout = P::sel(lane == il, P::shfl(D[S - 1], 31), sout);
@@ -822,7 +879,7 @@ size_t sdtw_smem_bytes(int precision, int cells_per_thread, int warps_per_cta) {
 }
 
 bool sdtw_instance_exists(int precision, int S, bool ref_del) {
-  if (ref_del) return precision == 1 && (S == 16 || S == 32);
+  if (ref_del) return (precision == 1 && (S == 16 || S == 32)) || (precision == 0 && S == 32);
   if (precision == 0) return S == 32 || S == 48;
   if (precision == 2) return S == 32 || S == 48 || S == 64;
   return S == 16 || S == 32 || S == 48;
@@ -832,6 +889,8 @@ bool sdtw_instance_exists(int precision, int S, bool ref_del) {
   if (precision == PREC && cells_per_thread == S) return CALL<S, PREC>
 #define DTWX_DISPATCH_RD(S, CALL) \
   if (precision == 1 && cells_per_thread == S) return CALL<S, 1, true>
+#define DTWX_DISPATCH_RD16(S, CALL) \
+  if (precision == 0 && cells_per_thread == S) return CALL<S, 0, true>
 #define DTWX_DISPATCH_ST16(S, CALL) \
   if (precision == 0 && cells_per_thread == S) return CALL<S, 0, false, true>
 
@@ -840,6 +899,7 @@ cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, 
   if (p.ref_del) {
     DTWX_DISPATCH_RD(16, launch_inst)(warps_per_cta, grid, p, tmap, s);
     DTWX_DISPATCH_RD(32, launch_inst)(warps_per_cta, grid, p, tmap, s);
+    DTWX_DISPATCH_RD16(32, launch_inst)(warps_per_cta, grid, p, tmap, s);
     return cudaErrorInvalidValue;
   }
   if (p.state_fp16) {
@@ -862,6 +922,7 @@ int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta, boo
   if (ref_del) {
     DTWX_DISPATCH_RD(16, occ_inst)(warps_per_cta);
     DTWX_DISPATCH_RD(32, occ_inst)(warps_per_cta);
+    DTWX_DISPATCH_RD16(32, occ_inst)(warps_per_cta);
     return 0;
   }
   DTWX_DISPATCH(0, 32, occ_inst)(warps_per_cta);

@@ -47,8 +47,8 @@ extern "C" {
 /* the recurrence */
 #define DTWX_NO_REF_DEL 0 /* D = d^2 + min(up, diag): the reference's build (-DNO_REF_DEL, src/Makefile:8) */
 #define DTWX_REF_DEL 1    /* D = d^2 + min(left, up, diag) (DTW.cu:23-29 without -DNO_REF_DEL);
-                             FP32 cells only; a read is one work item per strand (a
-                             horizontal run can cross any column chunk) */
+                             FP16 or FP32 cells; a read is one work item (per strand in
+                             FP32): a horizontal run can cross any column chunk */
 
 /* serving row state (the last DP row of a read between its chunks) */
 #define DTWX_STATE_FP32 0 /* absolute FP32 values: 8 bytes per column pair */

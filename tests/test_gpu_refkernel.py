@@ -275,3 +275,38 @@ def test_c1_calls_agree_with_reference_kernel(c1_tiles, oracle):
     # FP16 error) that rounding may order differently.  FP32 ends are exact
     # (test_gpu_sdtw.py).
     assert near_end[t].mean() >= 0.999
+
+
+def test_c1_ref_del_calls_agree_with_reference_kernel(oracle, built_lib):
+    """The REF_DEL builds side by side on the C1 shape on whole tiles: this
+    library's FP16 REF_DEL cells, the reference's FP16 REF_DEL kernel and the
+    FP64 REF_DEL oracle call the same reads at the FP64-tuned threshold."""
+    need("fp16_48128_rd")
+    import dtwax_gb300 as d
+    g = synth.random_genome(57 * TILE + 5, synth.GENOME_SEED)
+    o = synth.random_genome(57 * TILE + 5, synth.OTHER_SEED)
+    table = synth.level_table()
+    n = 256
+    mask = (np.arange(n) % 2 == 0).astype(np.int8)
+    reads = synth.simulate_reads(g, o, table, [QLEN] * n, mask, seed=synth.READ_SEED + 1)
+    with make_classifier(g, table, precision=d.FP16, recurrence=d.REF_DEL) as clf:
+        ours = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        fwd, rev = clf.reference()
+    z = zscore_reads(oracle, reads)
+    offs = np.arange(n + 1, dtype=np.int64) * QLEN
+    sf, ef, sr, er = oracle.sdtw_batch(fwd.astype(np.float64), rev.astype(np.float64),
+                                       z.reshape(-1).astype(np.float64), offs, ref_del=True)
+    with RK.RefKernel("fp16_48128_rd") as k:
+        tf, tr = k.run(k.reference(fwd, rev), z)
+    score64 = np.minimum(sf, sr)
+    theirs = np.minimum(tf, tr)
+    t = reads.target == 1
+    th, acc = threshold.best_threshold(score64[t], score64[~t], plateau="center")
+    c64, c_ours, c_theirs = (threshold.call(x, th) for x in (score64, ours["score"], theirs))
+    e_ours = rel(ours["score"], score64)
+    e_theirs = rel(theirs, score64)
+    print(f"\nC1 REF_DEL on whole tiles, 256 reads: ours FP16 vs FP64 max rel {e_ours.max():.2e}, reference "
+          f"FP16 vs FP64 max rel {e_theirs.max():.2e}; calls ours/FP64 {np.mean(c_ours == c64):.4f}, "
+          f"reference/FP64 {np.mean(c_theirs == c64):.4f}, ours/reference {np.mean(c_ours == c_theirs):.4f}")
+    assert e_ours.max() <= 1e-2
+    assert np.mean(c_ours == c64) >= 0.999 and np.mean(c_ours == c_theirs) >= 0.999

@@ -139,12 +139,39 @@ def test_ref_del_matches_oracle(lib, oracle, genome_pair, cells, warps):
     assert (plain[0] > ora[0]).any()
 
 
+def test_ref_del_fp16_matches_oracle(lib, oracle, genome_pair):
+    """REF_DEL on FP16 pairs with the running-minimum frames: within the FP16
+    tolerance of the FP64 REF_DEL oracle, end columns of target reads within 2."""
+    import dtwax_gb300 as d
+    g, o = genome_pair
+    tab = synth.level_table()
+    lengths = [2000, 1, 31, 32, 33, 1023, 1024, 1025, 2047, 2049, 3000, 500, 777, 64]
+    reads = reads_of_lengths(g, o, tab, lengths)
+    with make_classifier(g, tab, precision=d.FP16, recurrence=d.REF_DEL) as clf:
+        res = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        assert clf.tuning()["work_items"] == len(lengths)  # one item per read (both strands)
+    with make_classifier(g, tab, precision=d.FP32) as clf32:
+        fwd, rev = clf32.reference()
+    qs, offs = [], [0]
+    for r in range(reads.n):
+        z = oracle.zscore(reads.read(r).astype(np.float64), 1e-4).astype(np.float32).astype(np.float64)
+        qs.append(z)
+        offs.append(offs[-1] + z.size)
+    sf, ef, sr, er = oracle.sdtw_batch(fwd.astype(np.float64), rev.astype(np.float64), np.concatenate(qs),
+                                       np.array(offs, np.int64), ref_del=True)
+    np.testing.assert_allclose(res["score_fwd"], sf, rtol=FP16_RTOL, atol=1e-2)
+    np.testing.assert_allclose(res["score_rev"], sr, rtol=FP16_RTOL, atol=1e-2)
+    for i, n in enumerate(lengths):
+        if i % 2 == 0 and n >= 500:
+            best_end = ef[i] if sf[i] <= sr[i] else er[i]
+            assert abs(int(res["end_pos"][i]) - int(best_end)) <= 2
+
+
 def test_ref_del_rejects_other_cells(lib, genome_pair):
     import dtwax_gb300 as d
     g, _ = genome_pair
-    for prec in (d.FP16, d.MIXED):
-        with pytest.raises(d.DtwxError):
-            make_classifier(g, synth.level_table(), precision=prec, recurrence=d.REF_DEL)
+    with pytest.raises(d.DtwxError):
+        make_classifier(g, synth.level_table(), precision=d.MIXED, recurrence=d.REF_DEL)
 
 
 @pytest.mark.parametrize("cells,strips,warps", [(16, 1, 8), (32, 3, 2), (48, 2, 4), (32, 50, 1)])

@@ -50,7 +50,8 @@ def test_config_combinations_are_checked(built_lib, kat, tmp_path):
     c = d.default_config()
     assert c.recurrence == d.NO_REF_DEL and c.state_precision == d.STATE_FP32
     bad = [dict(precision=3), dict(recurrence=2), dict(state_precision=2),
-           dict(precision=d.FP16, recurrence=d.REF_DEL), dict(precision=d.MIXED, recurrence=d.REF_DEL),
+           dict(precision=d.FP16, recurrence=d.REF_DEL, state_precision=d.STATE_FP16),
+           dict(precision=d.MIXED, recurrence=d.REF_DEL),
            dict(precision=d.FP32, state_precision=d.STATE_FP16),
            dict(precision=d.FP32, recurrence=d.REF_DEL, cells_per_thread=48)]
     for kw in bad:
