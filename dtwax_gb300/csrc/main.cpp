@@ -19,7 +19,7 @@
 // Options:
 //   --fp32             FP32 cells (default FP16 half2 with running-min offset)
 //   --mixed            FP16 differences with FP32 path cost
-//   --ref-del          REF_DEL recurrence (left predecessor, FP32 cells)
+//   --ref-del          REF_DEL recurrence (left predecessor; FP16 or, with --fp32, FP32 cells)
 //   --threshold T      score below T calls "target" (default 194)
 //   --adapter N        samples skipped at the read start (default 1952, ADAPTER_LEN)
 //   --query-len N      samples aligned per read (default 2048, QUERY_LEN; 0 = rest)
@@ -187,7 +187,7 @@ int main(int argc, char **argv) {
     else if (a == "--mixed")
       cfg.precision = DTWX_MIXED;
     else if (a == "--ref-del")
-      cfg.recurrence = DTWX_REF_DEL, cfg.precision = DTWX_FP32;
+      cfg.recurrence = DTWX_REF_DEL;
     else if (a == "--threshold")
       cfg.threshold = (float)atof(next());
     else if (a == "--adapter")
