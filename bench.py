@@ -422,6 +422,9 @@ def run_ours(args, rank, world, local):
                    "raw samples resident in HBM", "l2": "flushed between timed steps (256 MB write)",
                    "tuning": tuning, "seeds": w.meta["seeds"], "parallelism": f"replicas x{world}"},
         "reads_per_s": reads_per_s,
+        # the reference's own secondary figure (hpc_helpers.hpp:93-100): samples
+        # per microsecond / 10, i.e. Mbases/s at 10 samples per base
+        "mbps": float(np.diff(w.reads.offsets).sum()) * world * args.steps / (total_ms * 1e3) / 10,
         "roofline": {"bound": "alu", "achieved": achieved, "peak": peak / 1e9, "unit": "Gcell/s",
                      "frac": achieved / (peak / 1e9), "traffic": traffic,
                      "peak_theoretical": theoretical, "frac_of_theoretical": achieved / theoretical,
