@@ -285,7 +285,8 @@ def run_reference(args, rank, world):
             "config": {"workload": f"{args.workload}: {WORKLOAD_DESC[args.workload]}", "implementation":
                        "oracle/sdtw_oracle.c: OpenMP FP64 restatement of scripts/sdtw.py sdtw_default "
                        "(numba original not installed); bounded read sample"},
-            "cpu_baseline": {k: rec[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "cpu_baseline": {k: rec[k] for k in ("value", "unit", "cores", "kind", "sample",
+                                                 "numpy_restatement_1core_gcups", "numba_original")},
             "e2e": {"value": rec["value"], "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "reads_per_s": rec["reads_per_s"]}
     if not args.skip_ref_gpu:
@@ -448,7 +449,8 @@ def run_ours(args, rank, world, local):
         line["config"]["workload"] += f" (first {n_reads} reads only)"
     if rank == 0:
         line["cpu_baseline"] = None if args.skip_cpu else {
-            k: v for k, v in cpu_baseline(w).items() if k in ("value", "unit", "cores", "kind", "sample")}
+            k: v for k, v in cpu_baseline(w).items()
+            if k in ("value", "unit", "cores", "kind", "sample", "numpy_restatement_1core_gcups", "numba_original")}
         print(json.dumps(line), flush=True)
     clf.close()
     if dist is not None:
