@@ -11,7 +11,7 @@
 // go to an optional side file (--side), one line per read:
 //   <idx>\t<read_id>\t<score>\t<end_pos>\t<strand: + or ->\t<call: target|non-target|skipped>
 //
-// Reads: FAST5 needs HDF5, which this build does not link, so the folder holds
+// Reads: FAST5 needs HDF5, which this library is not linked against, so the folder holds
 // one read per file as a 1-D numpy array (*.npy: int16 ADC or float32/float64
 // pA) or as whitespace-separated text samples (*.txt).  The read id is the file
 // name without its extension.  Files are taken in name order.
@@ -224,7 +224,7 @@ int main(int argc, char **argv) {
   std::vector<std::string> ids;
   for (const std::string &n : files) {
     if (ends_with(n, ".fast5")) {
-      std::cerr << "skipping " << n << ": FAST5 needs HDF5, which this build does not link\n";
+      std::cerr << "skipping " << n << ": FAST5 needs HDF5, which dtwx_main is not linked against\n";
       continue;
     }
     std::vector<float> s;

@@ -1,6 +1,6 @@
 """CPU oracle for the sDTW read-classification path.
 
-TEST INFRASTRUCTURE ONLY: the checker the CUDA library is compared against.
+TEST INFRASTRUCTURE ONLY: the oracle the CUDA library is compared against.
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may
 import this module.  The product package (dtwax_gb300) never imports it.
 

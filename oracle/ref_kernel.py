@@ -1,7 +1,7 @@
-"""The reference's own sDTW GPU kernel, built from its sources and run as a checker.
+"""The reference's own sDTW GPU kernel, built from its sources and run as a second oracle.
 
 TEST INFRASTRUCTURE ONLY.  Like the CPU oracle next to it, this module is a
-checker: only tests/ and bench.py's reference arm may import it, and the
+test oracle: only tests/ and bench.py's reference arm may import it, and the
 product package (dtwax_gb300) never does.
 
 * ``build()`` compiles oracle/ref_dtw_harness.cu, which includes the
@@ -9,7 +9,7 @@ product package (dtwax_gb300) never does.
   DTW.cu:151-572, with -DNO_REF_DEL as src/Makefile:8 sets it, or without it
   for the REF_DEL recurrence), into one device-only cubin per reference
   geometry under oracle/_ref/.  It needs the
-  reference's sources, so it runs only where they are (this build container);
+  reference's sources, so it runs only where they are present;
   the cubins travel with the repository and nothing else of the reference does.
 * ``RefKernel`` loads a cubin through the CUDA driver API (ctypes on
   libcuda), lays out the reference and the queries the way the reference's

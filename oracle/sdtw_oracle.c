@@ -1,7 +1,7 @@
 /*
  * FP64 CPU oracle for the subsequence-DTW (sDTW) read-classification path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker that the CUDA library
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle that the CUDA library
  * in dtwax_gb300/ is compared against.  Only tests/, __graft_entry__.smoke()
  * and the CPU-baseline leg of bench.py may load it; the product path never
  * links, loads or falls back to it.

@@ -1,6 +1,6 @@
 """Parity of the CUDA path with the FP64 oracle, through the C ABI.
 
-Tolerances (spec precision targets): FP32 scores within 1e-5 relative
+Tolerances (the precision targets): FP32 scores within 1e-5 relative
 of the FP64 oracle with the same end column; FP16 (half2 cells with the
 per-strip running-minimum offset) within 1e-2 relative.
 """
