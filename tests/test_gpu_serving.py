@@ -118,19 +118,21 @@ def test_fp16_state_halves_the_row_bytes(setup):
         make_classifier(g, tab, precision=d.FP32, state_precision=d.STATE_FP16)
 
 
-def test_resume_ref_del_matches_oracle(setup, oracle):
+@pytest.mark.parametrize("precision,rtol", [(1, 1e-5), (0, 1e-2)])
+def test_resume_ref_del_matches_oracle(setup, oracle, precision, rtol):
     """The REF_DEL recurrence resumed chunk by chunk from the saved rows."""
     import dtwax_gb300 as d
     g, o, tab, reads = setup
-    with make_classifier(g, tab, precision=d.FP32, recurrence=d.REF_DEL, threshold=-1.0) as clf:
+    with make_classifier(g, tab, precision=precision, recurrence=d.REF_DEL, threshold=-1.0) as clf:
         fwd, rev = clf.reference()
         chunks = {i: split(reads.read(i), 1600) for i in range(reads.n)}
         got = serve_reads(clf, chunks, chunks_per_decision=3)
     for i in range(reads.n):
         want = oracle_decisions(oracle, fwd.astype(np.float64), rev.astype(np.float64), chunks[i][:3], ref_del=True)
         for dd, (s, e, st) in zip(got[i], want):
-            assert dd["score"] == pytest.approx(s, rel=1e-5)
-            assert (dd["end_pos"], dd["strand"]) == (e, st)
+            assert dd["score"] == pytest.approx(s, rel=rtol)
+            if precision == 1:
+                assert (dd["end_pos"], dd["strand"]) == (e, st)
 
 
 @pytest.mark.parametrize("precision", [1, 0, 2])
