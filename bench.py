@@ -109,6 +109,15 @@ class ClockSampler:
                 "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
 
 
+def measured_hbm_gbs():
+    """Copy bandwidth measured on this machine's GPUs, when the file is present."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 def traffic_from_profile(precision: str):
     """DRAM bytes per sweep launch from the committed ncu summary, if present."""
     path = os.path.join(ROOT, "profiles", f"sdtw_{precision}_C2.md")
@@ -431,7 +440,11 @@ def run_ours(args, rank, world, local):
                      "peak_theoretical": theoretical, "frac_of_theoretical": achieved / theoretical,
                      "peak_source": "dtwx_peak_probe: the per-cell instruction mix (sub, min, fma) on "
                                     "register-resident cells, all SMs, measured in this run",
-                     "kernel": "dtwx::sdtw_kernel, mean of CUDA events around each launch"},
+                     "kernel": "dtwx::sdtw_kernel, mean of CUDA events around each launch",
+                     # the HBM roofline, for contrast: the sweep's measured DRAM traffic per
+                     # launch over its duration, against the measured copy bandwidth
+                     "hbm_achieved_gbs": (traffic / mean_sweep_s / 1e9) if traffic else None,
+                     "hbm_peak_gbs": measured_hbm_gbs()},
         "e2e": {"value": world * cells * len(e2e_ms) / (e2e_total / 1e3) / 1e9, "unit": "GCUPS",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "dtwx_classify_batch (host raw samples -> host results)"},
