@@ -118,9 +118,10 @@ def measured_hbm_gbs():
         return None
 
 
-def traffic_from_profile(precision: str):
-    """DRAM bytes per sweep launch from the committed ncu summary, if present."""
-    path = os.path.join(ROOT, "profiles", f"sdtw_{precision}_C2.md")
+def traffic_from_profile(precision: str, workload: str):
+    """DRAM bytes per sweep launch from the committed ncu summary of this
+    precision and workload, if present."""
+    path = os.path.join(ROOT, "profiles", f"sdtw_{precision}_{workload}.md")
     if not os.path.exists(path):
         return None
     m = re.search(r"dram_bytes_per_full_launch\s*=\s*([0-9.eE+]+)", open(path).read())
@@ -419,7 +420,7 @@ def run_ours(args, rank, world, local):
         # FP16 pairs take 6 FMA-pipe instructions (2 cycles each) per pair
         per_sm_cycle = 128.0 / 9.0 if precision == d.FP32 else 64.0 / 3.0
     theoretical = sms * per_sm_cycle * mhz * 1e6 / 1e9
-    traffic = traffic_from_profile(args.precision)
+    traffic = traffic_from_profile(args.precision, args.workload) if not ref_del else None
     t_mask = w.reads.target == 1
     line = {
         "metric": "sDTW GCUPS", "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
