@@ -114,6 +114,9 @@ _SIGNATURES = {
                                         ctypes.c_float]),
     "dtwx_submit_chunk": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_uint64, _P, ctypes.c_int32, ctypes.c_int32,
                                          ctypes.c_double]),
+    "dtwx_submit_chunk_i16": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_uint64, _P, ctypes.c_int32,
+                                             ctypes.c_int32, ctypes.c_double, ctypes.c_float, ctypes.c_float,
+                                             ctypes.c_float]),
     "dtwx_serve_step": (ctypes.c_int, [_P]),
     "dtwx_poll_decisions": (ctypes.c_int, [_P, ctypes.POINTER(Decision), ctypes.c_int32]),
     "dtwx_serve_drain": (ctypes.c_int, [_P]),
@@ -324,6 +327,14 @@ class Classifier:
         s = np.ascontiguousarray(samples, dtype=np.float32)
         _check(self._lib.dtwx_submit_chunk(self._h, channel, read_number, _ptr(s), s.size, int(is_last),
                                            float(arrival_ms)), self._h)
+
+    def submit_chunk_i16(self, channel: int, read_number: int, samples: np.ndarray, offset: float,
+                         range_: float, digitisation: float, is_last: bool = False, arrival_ms: float = -1.0):
+        """Raw int16 ADC chunk; pA = (raw + offset) * range / digitisation."""
+        s = np.ascontiguousarray(samples, dtype=np.int16)
+        _check(self._lib.dtwx_submit_chunk_i16(self._h, channel, read_number, _ptr(s), s.size, int(is_last),
+                                               float(arrival_ms), float(offset), float(range_),
+                                               float(digitisation)), self._h)
 
     def serve_step(self) -> int:
         return _check(self._lib.dtwx_serve_step(self._h), self._h)

@@ -1123,6 +1123,18 @@ int dtwx_serve_start(dtwx_handle *h, int32_t max_in_flight, double state_budget_
   return DTWX_OK;
 }
 
+int dtwx_submit_chunk_i16(dtwx_handle *h, int32_t channel, uint64_t read_number, const int16_t *samples,
+                          int32_t n, int32_t is_last, double arrival_ms, float offset, float range,
+                          float digitisation) {
+  if (!h) return DTWX_E_ARG;
+  if (n <= 0 || !samples) return fail(h, DTWX_E_ARG, "empty chunk");
+  if (!(digitisation != 0.f)) return fail(h, DTWX_E_ARG, "digitisation must be non-zero");
+  std::vector<float> pa((size_t)n);
+  const float mul = range / digitisation;
+  for (int32_t i = 0; i < n; ++i) pa[i] = ((float)samples[i] + offset) * mul;
+  return dtwx_submit_chunk(h, channel, read_number, pa.data(), n, is_last, arrival_ms);
+}
+
 int dtwx_submit_chunk(dtwx_handle *h, int32_t channel, uint64_t read_number, const float *samples, int32_t n,
                       int32_t is_last, double arrival_ms) {
   if (!h) return DTWX_E_ARG;

@@ -297,6 +297,13 @@ int dtwx_serve_start(dtwx_handle *h, int32_t max_in_flight, double state_budget_
 int dtwx_submit_chunk(dtwx_handle *h, int32_t channel, uint64_t read_number,
                       const float *samples, int32_t n, int32_t is_last, double arrival_ms);
 
+/* Same for raw int16 ADC samples as the sequencer delivers them
+ * (read_until/base.py:349 get_read_chunks, raw_data as int16):
+ * pA = (raw + offset) * range / digitisation (fast5/nanopolish_fast5_io.cpp:279-315). */
+int dtwx_submit_chunk_i16(dtwx_handle *h, int32_t channel, uint64_t read_number,
+                          const int16_t *samples, int32_t n, int32_t is_last, double arrival_ms,
+                          float offset, float range, float digitisation);
+
 /* Harvest finished batches and launch the next continuous batch if a chunk
  * is ready and fewer than serve_batches batches are in flight (never blocks);
  * returns the chunks launched (>= 0) or a status. */

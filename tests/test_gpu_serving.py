@@ -103,6 +103,31 @@ def test_resume_fp16_state_matches_oracle(setup, oracle):
                 assert dd["score"] == pytest.approx(s, rel=1e-2)
 
 
+def test_int16_chunks_match_float_chunks(setup):
+    """Raw int16 ADC chunks with their scaling give the decisions of the same
+    chunks converted to pA on the host."""
+    import dtwax_gb300 as d
+    g, o, tab, reads = setup
+    x = reads.read(0)
+    offset, rng_, digi = 12.0, 1400.0, 8192.0
+    raw = np.round(x * digi / rng_ - offset).astype(np.int16)
+    pa = ((raw.astype(np.float32) + offset) * (rng_ / digi)).astype(np.float32)
+    out = []
+    for use_i16 in (False, True):
+        with make_classifier(g, tab, precision=d.FP32, threshold=-1.0) as clf:
+            clf.serve_start(chunks_per_decision=3)
+            for k, lo in enumerate(range(0, 4800, 1600)):
+                last = lo + 1600 >= 4800
+                if use_i16:
+                    clf.submit_chunk_i16(1, 7, raw[lo:lo + 1600], offset, rng_, digi, is_last=last)
+                else:
+                    clf.submit_chunk(1, 7, pa[lo:lo + 1600], is_last=last)
+                clf.serve_step()
+            clf.serve_drain()
+            out.append([(dd["score"], dd["end_pos"]) for dd in clf.poll_decisions(100)])
+    assert out[0] == out[1] and len(out[0]) == 3
+
+
 def test_fp16_state_halves_the_row_bytes(setup):
     import dtwax_gb300 as d
     g, o, tab, reads = setup
