@@ -390,6 +390,18 @@ def test_cli_drop_in(lib, kat, tmp_path):
     np.testing.assert_allclose([float(r[4]) for r in rows], res["score_fwd"], rtol=1e-5)
     side_rows = [l.split("\t") for l in side.read_text().splitlines()]
     assert len(side_rows) == 5 and side_rows[-1][-1] == "skipped"
+    # the build variants as flags: same log shape, scores of the same handle options
+    for flags, kw, rtol in ((["--mixed"], dict(precision=d.MIXED), 1e-5),
+                            (["--ref-del"], dict(recurrence=d.REF_DEL), 1e-5),
+                            (["--fp32", "--ref-del"], dict(precision=d.FP32, recurrence=d.REF_DEL), 1e-5)):
+        out = subprocess.run([d.CLI_PATH, str(folder), model, fasta] + flags, capture_output=True, text=True,
+                             check=True).stdout.splitlines()
+        rows = [l.split("\t") for l in out[1:]]
+        assert len(rows) == 4 and all(len(r) == 6 for r in rows)
+        with d.Classifier(fasta=fasta, kmer_model=model, adapter_skip=1952, query_len=2048, require_full=1,
+                          **kw) as clf:
+            res = clf.classify([x.astype(np.float32) for x in raws])
+        np.testing.assert_allclose([float(r[4]) for r in rows], res["score_fwd"], rtol=rtol)
 
 
 def test_autotune_picks_a_compiled_shape_and_keeps_results(lib, genome_pair):
