@@ -286,8 +286,9 @@ def run_reference(args, rank, world):
         return 0
     w = synth.make_workload(args.workload)
     # each step is one pass over the bounded sample; warm-up passes are shorter
-    cpu_baseline(w, 1, target_s=2.0) if args.warmup > 0 else None
-    rec = cpu_baseline(w, n_steps=max(args.steps, 1), target_s=max(4.0, 60.0 / max(args.steps, 1)))
+    cpu_baseline(w, 1, target_s=min(2.0, args.cpu_seconds)) if args.warmup > 0 else None
+    rec = cpu_baseline(w, n_steps=max(args.steps, 1),
+                       target_s=max(min(4.0, args.cpu_seconds), args.cpu_seconds / max(args.steps, 1)))
     line = {"metric": "sDTW GCUPS", "value": rec["value"], "unit": "GCUPS", "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": rec["seconds"] * 1e3 / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -498,6 +499,8 @@ def main():
     ap.add_argument("--reads", type=int, default=0,
                     help="use only the first N reads of the workload (small cases for profiling)")
     ap.add_argument("--skip-cpu", action="store_true", help="do not time the CPU baseline")
+    ap.add_argument("--cpu-seconds", type=float, default=60.0,
+                    help="reference arm: CPU seconds over all timed steps (each step is a bounded read sample)")
     ap.add_argument("--serving", choices=["none", "C4", "C5"], default="C4",
                     help="Read Until serving simulation reported beside the batch metric")
     ap.add_argument("--serving-seconds", type=float, default=6.0)
