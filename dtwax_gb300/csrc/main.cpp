@@ -27,6 +27,22 @@
 //   --max-ref-len N    cap k-mer positions per strand (REF_LEN compatibility)
 //   --concat           score one sequence fwd||rev instead of the two strands
 //   --side FILE        write end position, strand and call per read
+//
+// Read Until FIFO mode, a drop-in for the reference's Read Until binary
+// `main <kmer_model> <ref.fasta> <pipe>` (src/ru_main.cu:67-326, fed by
+// src/ReadUntil/simulate_minion.py or ont_readuntil.py):
+//
+//   dtwx_main --fifo <kmer_model> <ref.fasta> <pipe> [--fp32|--mixed] [--ref-del] [--threshold T]
+//             [--reads N] [--query-len N]
+//
+// reads batches of N (default 10) reads x query-len (default 2,048) unsigned
+// 8-bit samples from the named pipe (generate_load_squiggle.hpp:303-343,
+// PIPE_SIZE = 10 x 2,048 at ru_main.cu:131-132) and prints, per read and with no
+// header, the line the reference prints (ru_main.cu:304-310):
+//   <idx>\t<idx>\t<QUERY_LEN>\t<REF_LEN>\t<fwd>\t<rev>
+// flushing after every batch.  It stops at the end of the stream (the reference
+// loops forever); a partial last batch is dropped, as the reference only
+// processes whole batches.
 #include <dirent.h>
 
 #include <algorithm>
@@ -156,6 +172,82 @@ bool load_txt(const std::string &path, std::vector<float> &out, std::string &err
   return true;
 }
 
+// The Read Until FIFO loop (see the header comment).
+int run_fifo(int argc, char **argv) {
+  if (argc < 5) {
+    std::cerr << "usage: dtwx_main --fifo <kmer_model> <ref.fasta> <pipe> [--fp32|--mixed] [--ref-del]\n"
+                 "       [--threshold T] [--reads N] [--query-len N]\n";
+    return 2;
+  }
+  const std::string model = argv[2], fasta = argv[3], pipe_path = argv[4];
+  dtwx_config cfg;
+  dtwx_config_default(&cfg);
+  int n_reads = 10, qlen = 2048;
+  for (int i = 5; i < argc; ++i) {
+    const std::string a = argv[i];
+    auto next = [&](void) -> const char * {
+      if (i + 1 >= argc) {
+        std::cerr << "missing value for " << a << "\n";
+        exit(2);
+      }
+      return argv[++i];
+    };
+    if (a == "--fp32")
+      cfg.precision = DTWX_FP32;
+    else if (a == "--mixed")
+      cfg.precision = DTWX_MIXED;
+    else if (a == "--ref-del")
+      cfg.recurrence = DTWX_REF_DEL;
+    else if (a == "--threshold")
+      cfg.threshold = (float)atof(next());
+    else if (a == "--reads")
+      n_reads = atoi(next());
+    else if (a == "--query-len")
+      qlen = atoi(next());
+    else {
+      std::cerr << "unknown option " << a << "\n";
+      return 2;
+    }
+  }
+  if (n_reads <= 0 || qlen <= 0) {
+    std::cerr << "--reads and --query-len must be positive\n";
+    return 2;
+  }
+  dtwx_handle *h = nullptr;
+  if (dtwx_create(&cfg, model.c_str(), nullptr, fasta.c_str(), &h) != DTWX_OK) {
+    std::cerr << "dtwx_create: " << dtwx_last_error(nullptr) << "\n";
+    return 1;
+  }
+  const int64_t ref_len = dtwx_ref_len(h);
+  std::ifstream pipe(pipe_path, std::ios::binary);
+  if (!pipe) {
+    std::cerr << "cannot open " << pipe_path << "\n";
+    dtwx_destroy(h);
+    return 1;
+  }
+  const size_t batch = (size_t)n_reads * (size_t)qlen;
+  std::vector<char> buf(batch);
+  std::vector<float> raw(batch);
+  std::vector<int64_t> offsets((size_t)n_reads + 1);
+  for (int r = 0; r <= n_reads; ++r) offsets[r] = (int64_t)r * qlen;
+  std::vector<dtwx_result> res((size_t)n_reads);
+  int rc = 0;
+  while (pipe.read(buf.data(), (std::streamsize)batch) && (size_t)pipe.gcount() == batch) {
+    for (size_t i = 0; i < batch; ++i) raw[i] = (float)(unsigned char)buf[i];
+    if (dtwx_classify_batch(h, raw.data(), offsets.data(), n_reads, res.data()) != DTWX_OK) {
+      std::cerr << "dtwx_classify_batch: " << dtwx_last_error(h) << "\n";
+      rc = 1;
+      break;
+    }
+    for (int j = 0; j < n_reads; ++j)
+      std::cout << j << "\t" << j << "\t" << qlen << "\t" << ref_len << "\t" << res[j].score_fwd << "\t"
+                << res[j].score_rev << "\n";
+    std::cout.flush();
+  }
+  dtwx_destroy(h);
+  return rc;
+}
+
 int usage() {
   std::cerr << "usage: dtwx_main <read_folder> <kmer_model> <ref.fasta> [--fp32|--mixed] [--ref-del] [--threshold T]\n"
                "       [--adapter N] [--query-len N] [--allow-short] [--max-ref-len N] [--concat] [--side FILE]\n";
@@ -165,6 +257,7 @@ int usage() {
 }  // namespace
 
 int main(int argc, char **argv) {
+  if (argc >= 2 && std::string(argv[1]) == "--fifo") return run_fifo(argc, argv);
   if (argc < 4) return usage();
   const std::string folder = argv[1], model = argv[2], fasta = argv[3];
   dtwx_config cfg;

@@ -404,6 +404,50 @@ def test_cli_drop_in(lib, kat, tmp_path):
         np.testing.assert_allclose([float(r[4]) for r in rows], res["score_fwd"], rtol=rtol)
 
 
+def test_cli_read_until_fifo(lib, kat, tmp_path):
+    """`dtwx_main --fifo <kmer_model> <ref.fasta> <pipe>`: the reference's Read
+    Until binary protocol (ru_main.cu, generate_load_squiggle.hpp:303-343).
+    Batches of 10 reads x 2,048 uint8 samples arrive on a named pipe, and one
+    6-token line per read comes back with the scores of dtwx_classify_batch."""
+    import os
+    import time
+    import dtwax_gb300 as d
+    fasta, model = write_kat_files(kat, str(tmp_path))
+    fifo = str(tmp_path / "pipe")
+    os.mkfifo(fifo)
+    rng = np.random.default_rng(9)
+    data = rng.integers(0, 256, size=2 * 10 * 2048, dtype=np.uint8)
+    proc = subprocess.Popen([d.CLI_PATH, "--fifo", model, fasta, fifo], stdout=subprocess.PIPE,
+                            stderr=subprocess.PIPE, text=True)
+    try:
+        # open for writing without blocking: wait (bounded) until the reader has opened the pipe
+        fd = None
+        t0 = time.time()
+        while fd is None and time.time() - t0 < 120 and proc.poll() is None:
+            try:
+                fd = os.open(fifo, os.O_WRONLY | os.O_NONBLOCK)
+            except OSError:
+                time.sleep(0.05)
+        assert fd is not None, proc.stderr.read() if proc.poll() is not None else "reader never opened the pipe"
+        os.set_blocking(fd, True)
+        os.write(fd, data.tobytes() + b"\x00" * 100)  # two whole batches and a partial one (dropped)
+        os.close(fd)
+        out, err = proc.communicate(timeout=120)
+    finally:
+        if proc.poll() is None:
+            proc.kill()
+    assert proc.returncode == 0, err
+    rows = [l.split("\t") for l in out.splitlines()]
+    assert len(rows) == 20 and all(len(r) == 6 for r in rows)
+    assert [r[0] for r in rows] == [str(j) for j in range(10)] * 2
+    with d.Classifier(fasta=fasta, kmer_model=model) as clf:
+        x = data.astype(np.float32)
+        res = clf.classify(raw=x, offsets=np.arange(21, dtype=np.int64) * 2048)
+        assert all(r[3] == str(clf.ref_len) for r in rows)
+    np.testing.assert_allclose([float(r[4]) for r in rows], res["score_fwd"], rtol=1e-5)
+    np.testing.assert_allclose([float(r[5]) for r in rows], res["score_rev"], rtol=1e-5)
+
+
 def test_autotune_picks_a_compiled_shape_and_keeps_results(lib, genome_pair):
     g, o = genome_pair
     tab = synth.level_table()
