@@ -72,3 +72,29 @@ def best_f1_threshold(target_scores, other_scores, num: int = 100000):
 def call(scores, threshold: float) -> np.ndarray:
     """1 = target (score < threshold), 0 = non-target."""
     return (np.asarray(scores) < threshold).astype(np.int8)
+
+
+def main(argv=None) -> int:
+    """`python -m dtwax_gb300.threshold <target_log> <other_log> [--plateau center]`:
+    the command line of calc_classification_threshold.py (microbial = target
+    log, human = other log), with the same three output lines."""
+    import argparse
+    ap = argparse.ArgumentParser(description="Calculate DTW classification accuracy thresholds")
+    ap.add_argument("microbial_file", help="path to the target (microbial) classification log")
+    ap.add_argument("human_file", help="path to the non-target (human) classification log")
+    ap.add_argument("--plateau", choices=["first", "center"], default="first",
+                    help="first: the reference's choice; center: the middle of the best-accuracy run")
+    args = ap.parse_args(argv)
+    with open(args.human_file) as f:
+        human = parse_log(f.read())
+    with open(args.microbial_file) as f:
+        microbial = parse_log(f.read())
+    print(len(microbial))
+    print(len(human))
+    th, acc = best_threshold(microbial, human, plateau=args.plateau)
+    print(f"Best classification threshold: {th}, accuracy: {acc}")
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

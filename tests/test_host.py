@@ -121,6 +121,31 @@ def test_threshold_tuner_on_reference_logs(score_logs):
     assert acc == pytest.approx(float(score_logs["ref_accuracy"]), rel=1e-12)
 
 
+def test_threshold_command_line(score_logs, tmp_path):
+    """`python -m dtwax_gb300.threshold <target_log> <other_log>` prints what
+    calc_classification_threshold.py prints for the same logs."""
+    import subprocess
+    import sys
+
+    def write(path, scores):
+        with open(path, "w") as f:
+            f.write("Read_ID\tQUERY_LEN\tREF_LEN\tsDTW score: fwd-strand\tsDTW score: rev-strand\n")
+            for i, v in enumerate(scores):
+                f.write(f"{i}\tr{i}\t2048\t48128\t{float(v)!r}\t{float(v) + 1.0!r}\n")
+
+    write(tmp_path / "t.log", score_logs["target"])
+    write(tmp_path / "o.log", score_logs["other"])
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, "-m", "dtwax_gb300.threshold", str(tmp_path / "t.log"),
+                          str(tmp_path / "o.log")], capture_output=True, text=True, check=True, cwd=root).stdout
+    lines = out.splitlines()
+    assert lines[0] == str(len(score_logs["target"])) and lines[1] == str(len(score_logs["other"]))
+    th = float(lines[2].split("threshold: ")[1].split(",")[0])
+    acc = float(lines[2].split("accuracy: ")[1])
+    assert th == pytest.approx(float(score_logs["ref_threshold"]), rel=1e-12)
+    assert acc == pytest.approx(float(score_logs["ref_accuracy"]), rel=1e-12)
+
+
 def test_parse_log_roundtrip(built_lib):
     import dtwax_gb300 as d
     from dtwax_gb300 import threshold
