@@ -2,7 +2,10 @@
 
 * ``parse_log`` reads the 6-column log of the CLI (src/main.cu:289-297) the way
   src/ReadUntil/calc_classification_threshold.py:5-33 does: header lines
-  (first token "Read_ID") are skipped and a read's score is min(fwd, rev).
+  (first token "Read_ID") are skipped and a read's score is min(fwd, rev).  It
+  also reads the CLI's extended side file (idx, read id, score, end column,
+  strand, call), whose fifth token is the strand sign; skipped reads are left
+  out.
 * ``best_threshold`` is the sweep of calc_classification_threshold.py:49-57:
   100,000 thresholds in linspace(0, max score); a target read is correct when
   its score < t, a non-target read when its score >= t; the first threshold of
@@ -23,6 +26,10 @@ def parse_log(text_or_lines) -> np.ndarray:
     for line in lines:
         t = line.split()
         if not t or t[0] == "Read_ID":
+            continue
+        if t[4] in ("+", "-"):  # extended side file
+            if t[5] != "skipped":
+                scores.append(float(t[2]))
             continue
         scores.append(min(float(t[4]), float(t[5])))
     return np.asarray(scores, np.float64)

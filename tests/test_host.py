@@ -121,6 +121,14 @@ def test_threshold_tuner_on_reference_logs(score_logs):
     assert acc == pytest.approx(float(score_logs["ref_accuracy"]), rel=1e-12)
 
 
+def test_parse_log_reads_the_side_file():
+    from dtwax_gb300 import threshold
+    side = "0\tr0\t12.5\t100\t+\ttarget\n1\tr1\t300.25\t7\t-\tnon-target\n2\tr2\tinf\t-1\t+\tskipped\n"
+    np.testing.assert_array_equal(threshold.parse_log(side), [12.5, 300.25])
+    log = "Read_ID\tQUERY_LEN\tREF_LEN\tfwd\trev\n0\tr0\t2048\t100\t5.5\t4.25\n"
+    np.testing.assert_array_equal(threshold.parse_log(log), [4.25])
+
+
 def test_threshold_command_line(score_logs, tmp_path):
     """`python -m dtwax_gb300.threshold <target_log> <other_log>` prints what
     calc_classification_threshold.py prints for the same logs."""
