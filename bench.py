@@ -467,13 +467,15 @@ def run_ours(args, rank, world, local):
         "check": {"target_score_per_sample_max": float((res["score"] / res["n_samples"])[t_mask].max()),
                   "other_score_per_sample_min": float((res["score"] / res["n_samples"])[~t_mask].min())},
     }
-    if args.serving != "none" and rank == 0:
+    # the serving run and the CPU baseline belong to the one-GPU line only: with
+    # N ranks every GPU would be held while rank 0 alone ran them
+    if args.serving != "none" and rank == 0 and world == 1:
         line["serving"] = run_serving(args.serving, precision, local, args.serving_seconds, args.serve_batches,
                                       args.state)
     if args.reads:
         line["config"]["workload"] += f" (first {n_reads} reads only)"
     if rank == 0:
-        line["cpu_baseline"] = None if args.skip_cpu else {
+        line["cpu_baseline"] = None if (args.skip_cpu or world > 1) else {
             k: v for k, v in cpu_baseline(w).items()
             if k in ("value", "unit", "cores", "kind", "sample", "numpy_restatement_1core_gcups", "numba_original")}
         print(json.dumps(line), flush=True)
