@@ -487,3 +487,40 @@ def test_cuda_graph_replay_matches_direct_launches(lib, genome_pair):
     for r in got:
         np.testing.assert_array_equal(r["score"], host["score"])
         np.testing.assert_array_equal(r["end_pos"], host["end_pos"])
+
+
+def test_full_size_properties_c3_genome(lib):
+    """Size-independent properties on the 5 Mb genome of the uneven-read
+    workload (where the FP64 oracle is too slow for every read): FP32 results
+    do not depend on the order of the reads in a batch, on how the batch is
+    split, on the launch shape, or on graph replay."""
+    import torch
+    import dtwax_gb300 as d
+    w = synth.make_workload("C3", n_reads=48)
+    raw, offs = w.reads.raw, w.reads.offsets
+    lens = np.diff(offs)
+    with make_classifier(w.genome, w.table, precision=d.FP32) as clf:
+        base = clf.classify(raw=raw, offsets=offs)
+        perm = np.random.default_rng(1).permutation(w.reads.n)
+        praw = np.concatenate([w.reads.read(i) for i in perm])
+        poffs = np.concatenate([[0], np.cumsum(lens[perm])]).astype(np.int64)
+        permuted = clf.classify(raw=praw, offsets=poffs)
+        half = w.reads.n // 2
+        first = clf.classify(raw=raw[: offs[half]], offsets=offs[: half + 1])
+        second = clf.classify(raw=raw[offs[half]:], offsets=offs[half:] - offs[half])
+    np.testing.assert_array_equal(permuted["score"], base["score"][perm])
+    np.testing.assert_array_equal(permuted["end_pos"], base["end_pos"][perm])
+    np.testing.assert_array_equal(np.concatenate([first["score"], second["score"]]), base["score"])
+    with make_classifier(w.genome, w.table, precision=d.FP32, cells_per_thread=16, warps_per_cta=8,
+                         use_graphs=1) as clf:
+        d_raw = torch.tensor(raw, device="cuda")
+        out = torch.zeros(32 * w.reads.n, dtype=torch.uint8, device="cuda")
+        s = torch.cuda.Stream()
+        got = []
+        for _ in range(3):  # direct, captured, replayed
+            clf.classify_device(d_raw.data_ptr(), offs, out.data_ptr(), s.cuda_stream)
+            s.synchronize()
+            got.append(np.frombuffer(out.cpu().numpy().tobytes(), d.RESULT_DTYPE).copy())
+    for g in got:
+        np.testing.assert_array_equal(g["score"], base["score"])
+        np.testing.assert_array_equal(g["end_pos"], base["end_pos"])
