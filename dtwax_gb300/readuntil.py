@@ -120,10 +120,11 @@ class SimulatedSequencer:
 
 
 def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget_bytes: float = 0.0,
-        max_in_flight: int = 0, drain: bool = False) -> dict:
+        max_in_flight: int = 0, drain: bool = False, sequencer: "SimulatedSequencer | None" = None) -> dict:
     """Real-time serving loop for warmup + duration seconds.  Returns the
     measured-window statistics.  Work still queued at the end is dropped
-    unless `drain` (an overloaded configuration can hold minutes of it)."""
+    unless `drain` (an overloaded configuration can hold minutes of it).
+    `sequencer` defaults to a SimulatedSequencer over `reads`."""
     from . import now_ms
 
     # serving batches hold a few chunk-steps each: tune the launch shape for them
@@ -131,7 +132,7 @@ def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget
         clf.autotune(k, cfg.chunk)
     clf.serve_start(max_in_flight=max_in_flight, state_budget_bytes=state_budget_bytes,
                     chunks_per_decision=cfg.chunks_per_read, accept_per_sample=accept, reject_per_sample=reject)
-    seq = SimulatedSequencer(reads, cfg)
+    seq = sequencer if sequencer is not None else SimulatedSequencer(reads, cfg)
     # no garbage-collector pauses inside the real-time loop
     gc_was_on = gc.isenabled()
     gc.disable()

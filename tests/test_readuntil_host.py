@@ -52,20 +52,9 @@ def test_loop_with_fake_library():
                                 read_rate=20.0)
     g, o = synth.random_genome(6000, 1), synth.random_genome(6000, 2)
     pool = readuntil.make_pool(g, o, synth.level_table(), cfg)
-    holder = {}
-    srv = FakeServer(lambda rn: holder["seq_truth"].get(rn, 0))
-    # route the fake's answers through the sequencer's own ground truth
-    orig = readuntil.SimulatedSequencer.__init__
-
-    def init(self, reads, c):
-        orig(self, reads, c)
-        holder["seq_truth"] = self.truth
-
-    readuntil.SimulatedSequencer.__init__ = init
-    try:
-        rec = readuntil.run(srv, pool, cfg, accept=0.1, reject=0.2)
-    finally:
-        readuntil.SimulatedSequencer.__init__ = orig
+    seq = readuntil.SimulatedSequencer(pool, cfg)
+    srv = FakeServer(lambda rn: seq.truth.get(rn, 0))  # answers with the sequencer's ground truth
+    rec = readuntil.run(srv, pool, cfg, accept=0.1, reject=0.2, sequencer=seq)
     assert rec["reads_per_s"] > 0 and rec["call_accuracy"] == 1.0
     assert rec["p50_latency_ms"] is not None and rec["p99_latency_ms"] >= rec["p50_latency_ms"] >= 0
     assert rec["accept_per_sample"] == 0.1 and rec["reject_per_sample"] == 0.2
