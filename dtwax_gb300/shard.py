@@ -28,9 +28,13 @@ def gather_results(local: np.ndarray, n: int, rank: int, world: int, group=None)
     raw = np.frombuffer(local.tobytes(), np.uint8)
     sizes = [shard_range(n, r, world)[1] - shard_range(n, r, world)[0] for r in range(world)]
     itemsize = local.dtype.itemsize
+    # NCCL gathers device tensors; gloo host tensors
+    device = "cuda" if dist.get_backend(group) == "nccl" else "cpu"
     buf = torch.zeros(max(sizes) * itemsize, dtype=torch.uint8)
     buf[: raw.size] = torch.from_numpy(raw.copy())
+    buf = buf.to(device)
     outs = [torch.zeros_like(buf) for _ in range(world)]
     dist.all_gather(outs, buf, group=group)
-    parts = [np.frombuffer(o.numpy().tobytes()[: sizes[r] * itemsize], local.dtype) for r, o in enumerate(outs)]
+    parts = [np.frombuffer(o.cpu().numpy().tobytes()[: sizes[r] * itemsize], local.dtype)
+             for r, o in enumerate(outs)]
     return np.concatenate(parts)
