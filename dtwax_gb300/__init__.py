@@ -310,10 +310,10 @@ class Classifier:
 
     def tuning(self):
         """Launch shape of the most recent batched sweep."""
-        v = (ctypes.c_int32 * 7)()
-        _check(self._lib.dtwx_get_tuning(self._h, v, 7), self._h)
+        v = (ctypes.c_int32 * 8)()
+        _check(self._lib.dtwx_get_tuning(self._h, v, 8), self._h)
         keys = ("cells_per_thread", "chunk_strips", "warps_per_cta", "ctas", "work_items", "ctas_per_sm",
-                "graph_replays")
+                "graph_replays", "narrow_halo")
         return dict(zip(keys, list(v)))
 
     # -- Read Until serving

@@ -40,6 +40,7 @@ struct Shape {
   int warps = 0;  // warps per CTA
   int grid = 0;   // CTAs
   int items = 0;
+  bool nh = false;  // narrow halo strips (FP16 pairs, narrow chunks)
 };
 
 // Buffers of one batch that may be in flight on its own stream.
@@ -197,12 +198,14 @@ bool make_tmap(CUtensorMap *map, void *base, int64_t bytes, int S, int ref_bytes
 
 // Analytic launch-shape model: with dynamic work stealing of equal-sized items
 // the sweep takes about ceil(items / warps) item times; an item of G strips
-// costs G strips plus the recomputed halo (about half of ceil(n/W) strips,
-// because halo strips stop at the last row that still reaches the chunk).
-int choose_chunk_strips(int64_t strips_per_read, int64_t n_tasks, double mean_rows, int W,
+// costs G strips plus the recomputed halo.  Halo strips (WH columns wide) stop
+// at the last row that still reaches the chunk, so the halo is about the
+// triangle n^2/2 rounded up to WH-wide steps: (n + WH) / (2 W) strips of W
+// columns, plus about 10 % for the per-row overhead of a narrow strip.
+int choose_chunk_strips(int64_t strips_per_read, int64_t n_tasks, double mean_rows, int W, int WH,
                         int64_t total_warps) {
   if (strips_per_read <= 1) return 1;
-  const double halo = std::ceil(mean_rows / W) * 0.55;
+  const double halo = (mean_rows + WH) / (2.0 * W) * (WH < W ? 1.1 : 1.0);
   double best_t = 1e300;
   int best_g = (int)strips_per_read;
   for (int64_t g = 1; g <= strips_per_read; ++g) {
@@ -268,11 +271,16 @@ Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_row
   } else if (f.G && !o.S) {
     s.G = f.G;
   } else {
-    const int g0 = choose_chunk_strips(strips, std::max<int64_t>(n_tasks, 1) * strands, mean_rows, W, total_warps);
+    // FP16 pairs: narrow chunks get the narrow-halo instance, so price their halo that way
+    const int64_t nt = std::max<int64_t>(n_tasks, 1) * strands;
+    int g0 = choose_chunk_strips(strips, nt, mean_rows, W, precision == 0 ? kWarp * kNarrowHaloCells : W,
+                                 total_warps);
+    if (precision == 0 && g0 > kNarrowHaloMaxStrips) g0 = choose_chunk_strips(strips, nt, mean_rows, W, W, total_warps);
     s.G = std::max(1, (int)std::lround(g0 * g_scale));
   }
   if (s.G > strips) s.G = (int)strips;
   const int64_t chunks = (strips + s.G - 1) / s.G;
+  s.nh = precision == 0 && !rd && chunks > 1 && s.G <= kNarrowHaloMaxStrips && s.S % kNarrowHaloCells == 0;
   const int64_t items = n_tasks * chunks * strands;
   s.items = (int)items;
   const int64_t want = (items + s.warps - 1) / s.warps;
@@ -334,6 +342,7 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
     p.strands = strands;
     p.ref_del = h->cfg.recurrence == DTWX_REF_DEL ? 1 : 0;
     p.state_fp16 = state_fp16(h) ? 1 : 0;
+    p.narrow_halo = sh.nh ? 1 : 0;
     const int ii = inst_index(precision, sh.S);
     p.use_tma = h->tmap_ok[precision][ii] ? 1 : 0;
     // inside a stream capture the timing events become event-record nodes
@@ -598,6 +607,7 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
       p.ref_del = h->cfg.recurrence == DTWX_REF_DEL ? 1 : 0;
       p.n_items = p.n_chunks * (precision != 0 ? p.strands : 1);
       p.ref_layout = 1;
+      p.narrow_halo = sh.nh ? 1 : 0;
       const int ii = inst_index(precision, sh.S);
       p.use_tma = h->tmap_ok[precision][ii] ? 1 : 0;
       CK(h, launch_sdtw(precision, sh.S, sh.warps, sh.grid, p, p.use_tma ? &h->tmap[precision][ii] : nullptr,
@@ -1031,12 +1041,12 @@ int dtwx_last_sweep_ms(dtwx_handle *h, float *ms) {
 int dtwx_get_tuning(const dtwx_handle *h, int32_t *out, int32_t n) {
   if (!h || !out || n < 0) return DTWX_E_ARG;
   const Shape &s = h->last_shape[h->cfg.precision];
-  const int32_t v[7] = {s.S, s.G, s.warps, s.grid, s.items,
+  const int32_t v[8] = {s.S, s.G, s.warps, s.grid, s.items,
                         s.S ? sdtw_ctas_per_sm(h->cfg.precision, s.S, s.warps,
                                                h->cfg.recurrence == DTWX_REF_DEL)
                             : 0,
-                        (int32_t)h->graph_replays};
-  for (int i = 0; i < n && i < 7; ++i) out[i] = v[i];
+                        (int32_t)h->graph_replays, s.nh ? 1 : 0};
+  for (int i = 0; i < n && i < 8; ++i) out[i] = v[i];
   return DTWX_OK;
 }
 

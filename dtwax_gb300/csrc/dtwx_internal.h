@@ -13,6 +13,18 @@ constexpr int kKmer = 6;
 constexpr int kTableSize = 4096;
 // Rows between two running-minimum rescales of the FP16 cells.
 constexpr int kRescaleRows = 32;
+
+// Narrow halo strips.  A column chunk starting at a > 0 recomputes a halo on
+// its left; the columns that still reach column a shrink by one per row, so
+// narrower halo strips stop sooner: 16-cell strips cut the halo of a
+// 1,600-row chunk from about 1.04 to 0.69 strips of 1,536 columns.  FP16-pair
+// kernels come in a second instance with such strips, launched when chunks
+// are narrow (at most kNarrowHaloMaxStrips strips, i.e. small batches) and
+// the halo is a large part of an item; wide-chunk batches keep the
+// full-width-halo instance, whose register allocation the halo loop would
+// otherwise change.
+constexpr int kNarrowHaloCells = 16;
+constexpr int kNarrowHaloMaxStrips = 32;
 // Bounded device-side waits: iterations before a wait gives up and flags an error.
 constexpr uint32_t kSpinLimit = 1u << 26;
 
@@ -63,6 +75,7 @@ struct SdtwParams {
   int32_t ref_del;             // 1: REF_DEL recurrence (left predecessor); needs one chunk per task
   int32_t state_fp16;          // FP16 cells: row state as half2 cells (m_pad) then one float2
                                // frame offset per 512-column group (m_pad / 512)
+  int32_t narrow_halo;         // FP16 pairs: launch the instance with kNarrowHaloCells-wide halo strips
 };
 
 // Per-warp scratch layout, in bytes, for cells of `pair_bytes` bytes.

@@ -19,7 +19,9 @@
 // scratch.  Chunks are independent: a chunk starting at a > 0 recomputes a
 // halo of >= n columns to its left, with +inf entering at the halo's left edge;
 // that error moves right one column per row, so it never reaches column a.
-// Halo strips stop at the last row that can still influence column a.
+// Halo strips stop at the last row that can still influence column a.  In the
+// NH instances they are narrower than the chunk's own strips, so the swept
+// halo follows that shrinking triangle more closely.
 //
 // FP16: cells are __half2 (fwd strand in .x, rev in .y).  Every kRescaleRows
 // rows each strip subtracts its own row minimum from its cells and adds it to
@@ -474,7 +476,8 @@ constexpr int sdtw_reg_cap() { return S + S * Pol<PREC>::RB / 4 + (RD ? 70 : 40)
 // column chunk, so the host gives REF_DEL tasks one chunk (no halo).
 // ST16: FP16 cells whose serving row state is FP16 (p.state_fp16); a separate
 // instance, so the other instances carry none of its registers.
-template <int S, int PREC, bool RD, bool ST16>
+// NH: halo strips kNarrowHaloCells wide (FP16 pairs, p.narrow_halo).
+template <int S, int PREC, bool RD, bool ST16, bool NH>
 __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
     const __grid_constant__ CUtensorMap tmap, const SdtwParams p) {
   using P = Pol<PREC>;
@@ -487,6 +490,10 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
   constexpr int CB = 4;                       // bytes per cell
   constexpr int STRIP_BYTES = W * RB;
   constexpr int K = kRescaleRows;
+  constexpr int SH = NH ? kNarrowHaloCells : S;  // cells per lane in halo strips
+  constexpr int WH = kWarp * SH;
+  static_assert(S % SH == 0 && SH % 8 == 0, "halo strips must tile the chunk start");
+  static_assert(!NH || (PREC == 0 && !RD), "narrow halo strips are built for FP16 pairs (REF_DEL has no halo)");
   static_assert(STRIP_BYTES % 1024 == 0, "strip tile must keep 1024-byte alignment");
   static_assert(S % 8 == 0, "row state and reference move in 16-byte groups");
   static_assert(!RD || PREC <= 1, "the REF_DEL row is built for FP16 pairs and FP32 cells");
@@ -547,12 +554,19 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
     }
     const int64_t a = (int64_t)chunk * C;
     const int64_t b = min(a + C, p.m);
-    int64_t x0 = 0;
+    // halo strips (left of a) are WH columns wide, the chunk's own strips W
+    int64_t x0 = a;
     if (chunk > 0) {
-      const int64_t halo = ((int64_t)n + W - 1) / W * W;
+      const int64_t halo = ((int64_t)n + WH - 1) / WH * WH;
       x0 = a - halo > 0 ? a - halo : 0;
     }
-    const int nstrips = (int)((b - x0 + W - 1) / W);
+    const int nh = (int)((a - x0) / WH);
+    const int nstrips = nh + (int)((b - a + W - 1) / W);
+    // strips [0, s_main) are narrow halo strips swept by sweep_halo_strip; the
+    // loop below sweeps the rest, W wide from column xm0 (with full-width halo
+    // strips it sweeps them too)
+    const int s_main = SH != S ? nh : 0;
+    const int64_t xm0 = SH != S ? a : x0;
     const float *q = p.query + t.q_off;
     const bool resume = (t.flags & kTaskResume) != 0;
     const bool save = (t.flags & kTaskSaveState) != 0 && p.state != nullptr;
@@ -569,8 +583,265 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
       tma_issue_if(slot0, &tmap, &bars[0], 0, (int)((ref_plane + x0) * RB / 128), STRIP_BYTES, is0);
     }
 
-    for (int s = 0; s < nstrips; ++s) {
-      const int64_t x = x0 + (int64_t)s * W;
+    // One narrow halo strip (SH cells per lane, left of column a); false if a
+    // TMA wait gave up.  The same steps as the loop below, without the
+    // result and row-state tail (a halo strip holds no output column).
+    auto sweep_halo_strip = [&](const int s) -> bool {
+      constexpr int NWH = SH * RB / 4;
+      const int64_t x = x0 + (int64_t)s * WH;
+      const bool relevant = false;
+      const bool first = (s == 0);
+        int rows = n;
+        if (!relevant) {
+          const int64_t lim = (int64_t)n - 1 - (a - x - WH);
+          rows = (int)(lim < 0 ? 0 : (lim > n ? n : lim));
+        }
+
+        // -- seam buffers (ping-pong by strip parity)
+        char *in_b = seam_base + ((s + 1) & 1) * seam_half;
+        char *out_b = seam_base + (s & 1) * seam_half;
+        const V *seam_in = reinterpret_cast<const V *>(in_b);
+        const float2 *off_in = reinterpret_cast<const float2 *>(in_b + off_pos);
+        V *seam_out = reinterpret_cast<V *>(out_b);
+        float2 *off_out = reinterpret_cast<float2 *>(out_b + off_pos);
+
+        // -- initial row ("row -1"): zeros (free start) or the saved row state
+        V D[SH];
+        float2 O = make_float2(0.f, 0.f);  // FP16 frame offsets (fwd, rev)
+        if (resume) {
+          const int64_t c0 = x + (int64_t)lane * SH;
+          if constexpr (PREC == 0) {
+            if constexpr (ST16) {
+              // FP16 row state: half2 cells relative to the offset of their
+              // 512-column group (the saving strip's frame); re-based onto this
+              // strip's minimum
+              const uint4 *hc = reinterpret_cast<const uint4 *>(reinterpret_cast<const __half2 *>(st_plane0) + c0);
+              const float2 *og = reinterpret_cast<const float2 *>(st_plane0 + p.m_pad);
+  #pragma unroll
+              for (int k = 0; k < SH / 4; ++k) {
+                const uint4 u = hc[k];
+                D[4 * k] = bits_as<__half2>(u.x);
+                D[4 * k + 1] = bits_as<__half2>(u.y);
+                D[4 * k + 2] = bits_as<__half2>(u.z);
+                D[4 * k + 3] = bits_as<__half2>(u.w);
+              }
+              float mx = __int_as_float(0x7f800000), my = mx;
+  #pragma unroll
+              for (int k = 0; k < SH; ++k) {
+                const float2 o = og[(c0 + k) >> 9];
+                const float2 v = __half22float2(D[k]);
+                mx = fminf(mx, v.x + o.x);
+                my = fminf(my, v.y + o.y);
+              }
+  #pragma unroll
+              for (int m = 16; m >= 1; m >>= 1) {
+                mx = fminf(mx, __shfl_xor_sync(FULL_MASK, mx, m));
+                my = fminf(my, __shfl_xor_sync(FULL_MASK, my, m));
+              }
+              O = make_float2(mx, my);
+  #pragma unroll
+              for (int k = 0; k < SH; ++k) {
+                const float2 o = og[(c0 + k) >> 9];
+                const float2 v = __half22float2(D[k]);
+                D[k] = __floats2half2_rn(v.x + o.x - mx, v.y + o.y - my);
+              }
+            } else {
+            // two passes over the saved planes: strip minimum first, then the cells
+            const float4 *f0 = reinterpret_cast<const float4 *>(st_plane0 + c0);
+            const float4 *f1 = reinterpret_cast<const float4 *>(st_plane0 + p.m_pad + c0);
+            float mx = __int_as_float(0x7f800000), my = mx;
+  #pragma unroll
+            for (int k = 0; k < SH / 4; ++k) {
+              const float4 u = f0[k], v = f1[k];
+              mx = fminf(mx, fminf(fminf(u.x, u.y), fminf(u.z, u.w)));
+              my = fminf(my, fminf(fminf(v.x, v.y), fminf(v.z, v.w)));
+            }
+  #pragma unroll
+            for (int m = 16; m >= 1; m >>= 1) {
+              mx = fminf(mx, __shfl_xor_sync(FULL_MASK, mx, m));
+              my = fminf(my, __shfl_xor_sync(FULL_MASK, my, m));
+            }
+            O = make_float2(mx, my);
+  #pragma unroll
+            for (int k = 0; k < SH / 4; ++k) {
+              const float4 u = f0[k], v = f1[k];
+              D[4 * k] = __floats2half2_rn(u.x - mx, v.x - my);
+              D[4 * k + 1] = __floats2half2_rn(u.y - mx, v.y - my);
+              D[4 * k + 2] = __floats2half2_rn(u.z - mx, v.z - my);
+              D[4 * k + 3] = __floats2half2_rn(u.w - mx, v.w - my);
+            }
+            }
+          } else {
+            const float4 *f = reinterpret_cast<const float4 *>(st_plane0 + (int64_t)strand * p.m_pad + c0);
+  #pragma unroll
+            for (int k = 0; k < SH / 4; ++k) {
+              const float4 u = f[k];
+              D[4 * k] = u.x;
+              D[4 * k + 1] = u.y;
+              D[4 * k + 2] = u.z;
+              D[4 * k + 3] = u.w;
+            }
+          }
+        } else {
+  #pragma unroll
+          for (int k = 0; k < SH; ++k) D[k] = P::zero();
+        }
+
+        // -- reference strip into registers (after the row state: fewer live registers)
+        RV R[NWH];
+        if (p.use_tma) {
+          const int sl = s & 1;
+          // every lane waits (acquire of the TMA bytes); the give-up decision is warp-uniform
+          const bool ok = __all_sync(FULL_MASK, mbar_wait(&bars[sl], (phase >> sl) & 1u));
+          if (!ok) {
+            atomicOr(p.err, kErrTmaTimeout);  // every lane: same bit
+            return false;
+          }
+          phase ^= 1u << sl;
+          regs_from_smem<NWH, RV>(slot0 + sl * STRIP_BYTES, lane, R);
+          __syncwarp();
+          if (s + 1 < nstrips) {
+            const int ns = (s + 1) & 1;
+            fence_proxy_async_smem();
+            tma_issue_if(slot0 + ns * STRIP_BYTES, &tmap, &bars[ns], 0,
+                         (int)((ref_plane + (s + 1 < nh ? x + WH : a)) * RB / 128),
+                         STRIP_BYTES, is0);
+          }
+        } else if constexpr (PREC == 1) {
+          if (p.ref_layout == 0)
+            regs_from_pairs<SH>(reinterpret_cast<const float2 *>(p.ref_plain), x, lane, strand, R);
+          else
+            regs_from_global<NWH, RV>(reinterpret_cast<const float *>(p.ref_plain) + ref_plane + x, lane, R);
+        } else if constexpr (PREC == 2) {
+          regs_from_global<NWH, RV>(reinterpret_cast<const __half *>(p.ref_plain) + ref_plane + x, lane, R);
+        } else {
+          regs_from_global<NWH, RV>(reinterpret_cast<const __half2 *>(p.ref_plain) + x, lane, R);
+        }
+
+        // uniform stores (every lane writes the same value): no lane-dependent branch
+        seam_out[0] = P::shfl(D[SH - 1], 31);
+        if constexpr (PREC == 0) off_out[0] = O;
+
+        // offset of this strip's frame relative to the left strip's frame (FP16)
+        V delta = P::zero();
+        float2 off_next = make_float2(0.f, 0.f);
+        if constexpr (PREC == 0) {
+          if (!first) {
+            const float2 oi = off_in[0];
+            delta = __float22half2_rn(make_float2(oi.x - O.x, oi.y - O.y));
+            if (n >= K) off_next = off_in[1];
+          }
+        }
+
+        // -- row sweep, 32 rows per window: lane l holds query sample i0+l and
+        // the incoming seam value of row i0+l, already re-based into this strip's
+        // frame (delta changes only at a rescale, which ends a window)
+        const V vinf = P::inf();
+        typename P::QW qwin = P::qw(lane < n ? q[lane] : 0.f);
+        // REF_DEL also reads the seam value of the last row itself (one entry further)
+        constexpr int kExtra = RD ? 1 : 0;
+        V swin = (!first && lane < rows + kExtra) ? seam_in[lane] : vinf;
+        if constexpr (PREC == 0) swin = __hadd2(swin, delta);
+        V *so = seam_out + 1;  // seam value of row i goes to seam_out[i + 1]
+        for (int i0 = 0; i0 < rows; i0 += kWarp) {
+          const int r = i0 + kWarp + lane;
+          const float qn = r < n ? q[r] : 0.f;
+          const V sn = (!first && r < rows + kExtra) ? seam_in[r] : vinf;
+          // the seam column leaving this strip is gathered in a register window
+          // (lane l keeps row i0+l) and stored once per 32 rows, coalesced: no
+          // lane-conditional store inside the row loop
+          V sout = vinf;
+          // REF_DEL: lane l of lwin holds the left strip's value on row i0+l itself
+          V lwin = vinf;
+          if constexpr (RD) {
+            V last = P::shfl(sn, 0);  // the left strip's value on row i0+31, stored after its rescale
+            if constexpr (PREC == 0) {
+              // that value is in the left strip's next frame: re-base with the next epoch's offset
+              last = __hadd2(last, __float22half2_rn(make_float2(off_next.x - O.x, off_next.y - O.y)));
+            }
+            lwin = P::sel(lane == kWarp - 1, last, __shfl_down_sync(FULL_MASK, swin, 1));
+          }
+          if (rows - i0 >= kWarp) {
+  #pragma unroll 4
+            for (int il = 0; il < kWarp; ++il) {
+              if constexpr (RD)
+                row_refdel<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
+              else
+                row<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+              if constexpr (SMEM_SEAM)
+                st_shared_if(sob + 4u * (uint32_t)il, cell_bits<PREC>(D[SH - 1]), is31);
+              else
+                sout = P::sel(lane == il, P::shfl(D[SH - 1], 31), sout);
+            }
+            if constexpr (PREC == 0) {
+              // rescale: subtract this strip's row minimum (one epoch = 32 rows)
+              V mn = D[0];
+  #pragma unroll
+              for (int k = 1; k < SH; ++k) mn = __hmin2(mn, D[k]);
+  #pragma unroll
+              for (int m = 16; m >= 1; m >>= 1) mn = __hmin2(mn, P::shfl_xor(mn, m));
+  #pragma unroll
+              for (int k = 0; k < SH; ++k) D[k] = __hsub2(D[k], mn);
+              const float2 mf = __half22float2(mn);
+              O.x += mf.x;
+              O.y += mf.y;
+              const int e = (i0 + kWarp) / K;
+              off_out[e] = O;  // warp-uniform value, stored by every lane
+              sout = P::sel(lane == kWarp - 1, P::shfl(D[SH - 1], 31), sout);  // the seam leaves in the new frame
+              if (!first) {
+                delta = __float22half2_rn(make_float2(off_next.x - O.x, off_next.y - O.y));
+                if ((e + 1) * K <= n) off_next = off_in[e + 1];
+              }
+            }
+            if constexpr (SMEM_SEAM) {
+              __syncwarp();
+              sout = P::from_bits(ld_shared_u32(sob + 4u * (uint32_t)lane));
+              __syncwarp();
+            }
+            so[lane] = sout;
+          } else {
+            const int cnt = rows - i0;
+            for (int il = 0; il < cnt; ++il) {
+              if constexpr (RD)
+                row_refdel<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
+              else
+                row<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+              if constexpr (SMEM_SEAM)
+                st_shared_if(sob + 4u * (uint32_t)il, cell_bits<PREC>(D[SH - 1]), is31);
+              else
+                sout = P::sel(lane == il, P::shfl(D[SH - 1], 31), sout);
+            }
+            if constexpr (SMEM_SEAM) {
+              __syncwarp();
+              sout = lane < cnt ? P::from_bits(ld_shared_u32(sob + 4u * (uint32_t)lane)) : vinf;
+              __syncwarp();
+            }
+            so[lane] = sout;  // lanes >= cnt write +inf into the buffer's 32-entry slack past the rows
+          }
+          so += kWarp;
+          qwin = P::qw(qn);
+          swin = sn;
+          if constexpr (PREC == 0) swin = __hadd2(swin, delta);
+        }
+        if (rows < n) {
+          // rows this halo strip skipped can no longer reach column a: keep them
+          // inert (whole 32-entry groups; the buffers have 32 entries of slack)
+          for (int rr = rows + 1; rr <= n; rr += kWarp) seam_out[rr + lane] = vinf;
+          if constexpr (PREC == 0) {
+            for (int e = rows / K + 1; e <= n / K; e += kWarp) off_out[e + lane] = O;
+          }
+        }
+        __syncwarp();
+
+      return true;
+    };
+    if constexpr (SH != S) {
+      for (int s = 0; s < nh; ++s)
+        if (!sweep_halo_strip(s)) return;
+    }
+
+    for (int s = s_main; s < nstrips; ++s) {
+      const int64_t x = xm0 + (int64_t)(s - s_main) * W;
       const bool relevant = x >= a;
       const bool first = (s == 0);
       int rows = n;
@@ -880,11 +1151,11 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
 
 // ---------------------------------------------------------------- instances / launch
 
-template <int S, int PREC, bool RD = false, bool ST16 = false>
+template <int S, int PREC, bool RD = false, bool ST16 = false, bool NH = false>
 static cudaError_t launch_inst(int warps, int grid, const SdtwParams &p, const CUtensorMap *tmap,
                                cudaStream_t s) {
   const size_t smem = sdtw_smem_bytes(PREC, S, warps);
-  auto fn = sdtw_kernel<S, PREC, RD, ST16>;
+  auto fn = sdtw_kernel<S, PREC, RD, ST16, NH>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   CUtensorMap dummy;
@@ -896,11 +1167,11 @@ static cudaError_t launch_inst(int warps, int grid, const SdtwParams &p, const C
   return cudaGetLastError();
 }
 
-template <int S, int PREC, bool RD = false, bool ST16 = false>
+template <int S, int PREC, bool RD = false, bool ST16 = false, bool NH = false>
 static int occ_inst(int warps) {
   int n = 0;
   const size_t smem = sdtw_smem_bytes(PREC, S, warps);
-  auto fn = sdtw_kernel<S, PREC, RD, ST16>;
+  auto fn = sdtw_kernel<S, PREC, RD, ST16, NH>;
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, warps * kWarp, smem) != cudaSuccess) return 0;
@@ -931,6 +1202,8 @@ bool sdtw_instance_exists(int precision, int S, bool ref_del) {
   if (precision == 0 && cells_per_thread == S) return CALL<S, 0, true>
 #define DTWX_DISPATCH_ST16(S, CALL) \
   if (precision == 0 && cells_per_thread == S) return CALL<S, 0, false, true>
+#define DTWX_DISPATCH_NH(S, ST16, CALL) \
+  if (precision == 0 && cells_per_thread == S) return CALL<S, 0, false, ST16, true>
 
 cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, int grid,
                         const SdtwParams &p, const CUtensorMap *tmap, cudaStream_t s) {
@@ -938,6 +1211,16 @@ cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, 
     DTWX_DISPATCH_RD(16, launch_inst)(warps_per_cta, grid, p, tmap, s);
     DTWX_DISPATCH_RD(32, launch_inst)(warps_per_cta, grid, p, tmap, s);
     DTWX_DISPATCH_RD16(32, launch_inst)(warps_per_cta, grid, p, tmap, s);
+    return cudaErrorInvalidValue;
+  }
+  if (p.narrow_halo) {
+    if (p.state_fp16) {
+      DTWX_DISPATCH_NH(32, true, launch_inst)(warps_per_cta, grid, p, tmap, s);
+      DTWX_DISPATCH_NH(48, true, launch_inst)(warps_per_cta, grid, p, tmap, s);
+    } else {
+      DTWX_DISPATCH_NH(32, false, launch_inst)(warps_per_cta, grid, p, tmap, s);
+      DTWX_DISPATCH_NH(48, false, launch_inst)(warps_per_cta, grid, p, tmap, s);
+    }
     return cudaErrorInvalidValue;
   }
   if (p.state_fp16) {

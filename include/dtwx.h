@@ -220,18 +220,19 @@ int32_t dtwx_last_launch_count(const dtwx_handle *h);
  * figure with TIMERSTOP_CUDA (src/include/hpc_helpers.hpp:93-100). */
 int dtwx_last_sweep_ms(dtwx_handle *h, float *ms);
 
-/* Autotuner: time the sweep on a synthetic batch of min(n_reads, 1024) reads
- * of read_len samples for every compiled cells-per-thread instance, 4 and 8
- * warps per CTA, and half / once / twice the analytic chunk width; the fastest
- * shape is used from then on for batches of n_reads reads of that length (log2
- * buckets of read count and read length).  *best_ms gets its sweep time.  The reference fixes these
- * at compile time (SEGMENT_SIZE, BLOCK_NUM; src/include/common.hpp:64-79). */
+/* Autotuner: time the sweep on a synthetic batch of n_reads reads of read_len
+ * samples (cut to at most 2,048 reads and about 1.2e13 cells) for every
+ * compiled cells-per-thread instance, 4 and 8 warps per CTA, and half / once /
+ * twice the analytic chunk width; the fastest shape is used from then on for
+ * batches of n_reads reads of that length (log2 buckets of read count and
+ * read length).  *best_ms gets its sweep time.  The reference fixes these at
+ * compile time (SEGMENT_SIZE, BLOCK_NUM; src/include/common.hpp:64-79). */
 int dtwx_autotune(dtwx_handle *h, int32_t n_reads, int32_t read_len, float *best_ms);
 
 /* Launch shape of the handle's most recent batched sweep in its precision:
  * out[0..n) = cells per thread, strips per work item, warps per CTA, CTAs,
- * work items, resident CTAs per SM, CUDA-graph replays so far (as many as n
- * asks for, up to 7). */
+ * work items, resident CTAs per SM, CUDA-graph replays so far, 1 if the
+ * narrow-halo kernel instance ran (as many as n asks for, up to 8). */
 int dtwx_get_tuning(const dtwx_handle *h, int32_t *out, int32_t n);
 
 /* Measured issue-rate ceiling of the cell update on this device: a kernel that

@@ -212,16 +212,25 @@ def test_mixed_chunking_is_exact(lib, genome_pair, cells, strips, warps):
     np.testing.assert_array_equal(res["end_pos"], base["end_pos"])
 
 
-@pytest.mark.parametrize("cells,strips", [(32, 1), (48, 2), (32, 7)])
+@pytest.mark.parametrize("cells,strips", [(32, 1), (48, 2), (32, 7), (48, 13)])
 def test_fp16_chunking_within_tolerance(lib, oracle, genome_pair, cells, strips):
+    """Narrow chunks run the kernel instance with 16-cell halo strips (the
+    3,100-sample read's halo reaches column 0 for the first chunks); one chunk
+    per read (13 strips of 1,536 columns) has no halo."""
     g, o = genome_pair
     tab = synth.level_table()
     reads = reads_of_lengths(g, o, tab, [1500, 2000, 2500, 3100])
     with make_classifier(g, tab, precision=0, cells_per_thread=cells, chunk_strips=strips) as clf:
         res = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        t = clf.tuning()
         sf, ef, sr, er = oracle_classify(oracle, clf, reads.raw, reads.offsets)
+    strips_per_read = -(-(len(g) - 5) // (32 * cells))
+    assert t["narrow_halo"] == (1 if strips < strips_per_read else 0)
     np.testing.assert_allclose(res["score_fwd"], sf, rtol=FP16_RTOL)
     np.testing.assert_allclose(res["score_rev"], sr, rtol=FP16_RTOL)
+    for i in (0, 2):  # target reads: end column within 2 of the oracle's
+        best_end = ef[i] if sf[i] <= sr[i] else er[i]
+        assert abs(int(res["end_pos"][i]) - int(best_end)) <= 2
 
 
 @pytest.mark.parametrize("precision", [1, 0])
