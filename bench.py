@@ -204,6 +204,12 @@ def run_serving(name: str, precision: int, device: int, duration_s: float, batch
                       serve_batches=batches, state_precision=state_precision) as clf:
         accept, reject = readuntil.calibrate(clf, reads, cfg)
         rec = readuntil.run(clf, reads, cfg, accept, reject, state_budget_bytes=spec["budget_gb"] * 1e9)
+    # row-state traffic of the resumed sweeps: a slot holds both strands' last
+    # DP row (8 B per column pair in FP32, about 4 B with FP16 rows); each
+    # chunk-step reads it (except a read's first chunk) and writes it back
+    slot_bytes = (4 if state_precision == d.STATE_FP16 else 8) * (spec["genome_len"] - 5)
+    rec["row_state_gbs"] = rec["chunks_processed_per_s"] * 2 * slot_bytes / 1e9
+    rec["row_state_bytes_per_chunk_step"] = 2 * slot_bytes
     rec["workload"] = (f"{name}: {spec['channels']} channels, 1,600-sample chunks every 0.4 s, Poisson read "
                        f"starts 1/s/channel, <= 3 chunks per decision, {spec['genome_len'] // 1_000_000} Mb "
                        f"seeded genome ({2 * (spec['genome_len'] - 5)} columns), row-state budget "
