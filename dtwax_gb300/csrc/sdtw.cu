@@ -589,72 +589,46 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
     auto sweep_halo_strip = [&](const int s) -> bool {
       constexpr int NWH = SH * RB / 4;
       const int64_t x = x0 + (int64_t)s * WH;
-      const bool relevant = false;
       const bool first = (s == 0);
-        int rows = n;
-        if (!relevant) {
-          const int64_t lim = (int64_t)n - 1 - (a - x - WH);
-          rows = (int)(lim < 0 ? 0 : (lim > n ? n : lim));
-        }
+      // rows that can still reach column a
+      const int64_t lim = (int64_t)n - 1 - (a - x - WH);
+      const int rows = (int)(lim < 0 ? 0 : (lim > n ? n : lim));
 
-        // -- seam buffers (ping-pong by strip parity)
-        char *in_b = seam_base + ((s + 1) & 1) * seam_half;
-        char *out_b = seam_base + (s & 1) * seam_half;
-        const V *seam_in = reinterpret_cast<const V *>(in_b);
-        const float2 *off_in = reinterpret_cast<const float2 *>(in_b + off_pos);
-        V *seam_out = reinterpret_cast<V *>(out_b);
-        float2 *off_out = reinterpret_cast<float2 *>(out_b + off_pos);
+      // -- seam buffers (ping-pong by strip parity)
+      char *in_b = seam_base + ((s + 1) & 1) * seam_half;
+      char *out_b = seam_base + (s & 1) * seam_half;
+      const V *seam_in = reinterpret_cast<const V *>(in_b);
+      const float2 *off_in = reinterpret_cast<const float2 *>(in_b + off_pos);
+      V *seam_out = reinterpret_cast<V *>(out_b);
+      float2 *off_out = reinterpret_cast<float2 *>(out_b + off_pos);
 
-        // -- initial row ("row -1"): zeros (free start) or the saved row state
-        V D[SH];
-        float2 O = make_float2(0.f, 0.f);  // FP16 frame offsets (fwd, rev)
-        if (resume) {
-          const int64_t c0 = x + (int64_t)lane * SH;
-          if constexpr (PREC == 0) {
-            if constexpr (ST16) {
-              // FP16 row state: half2 cells relative to the offset of their
-              // 512-column group (the saving strip's frame); re-based onto this
-              // strip's minimum
-              const uint4 *hc = reinterpret_cast<const uint4 *>(reinterpret_cast<const __half2 *>(st_plane0) + c0);
-              const float2 *og = reinterpret_cast<const float2 *>(st_plane0 + p.m_pad);
-  #pragma unroll
-              for (int k = 0; k < SH / 4; ++k) {
-                const uint4 u = hc[k];
-                D[4 * k] = bits_as<__half2>(u.x);
-                D[4 * k + 1] = bits_as<__half2>(u.y);
-                D[4 * k + 2] = bits_as<__half2>(u.z);
-                D[4 * k + 3] = bits_as<__half2>(u.w);
-              }
-              float mx = __int_as_float(0x7f800000), my = mx;
-  #pragma unroll
-              for (int k = 0; k < SH; ++k) {
-                const float2 o = og[(c0 + k) >> 9];
-                const float2 v = __half22float2(D[k]);
-                mx = fminf(mx, v.x + o.x);
-                my = fminf(my, v.y + o.y);
-              }
-  #pragma unroll
-              for (int m = 16; m >= 1; m >>= 1) {
-                mx = fminf(mx, __shfl_xor_sync(FULL_MASK, mx, m));
-                my = fminf(my, __shfl_xor_sync(FULL_MASK, my, m));
-              }
-              O = make_float2(mx, my);
-  #pragma unroll
-              for (int k = 0; k < SH; ++k) {
-                const float2 o = og[(c0 + k) >> 9];
-                const float2 v = __half22float2(D[k]);
-                D[k] = __floats2half2_rn(v.x + o.x - mx, v.y + o.y - my);
-              }
-            } else {
-            // two passes over the saved planes: strip minimum first, then the cells
-            const float4 *f0 = reinterpret_cast<const float4 *>(st_plane0 + c0);
-            const float4 *f1 = reinterpret_cast<const float4 *>(st_plane0 + p.m_pad + c0);
-            float mx = __int_as_float(0x7f800000), my = mx;
+      // -- initial row ("row -1"): zeros (free start) or the saved row state
+      V D[SH];
+      float2 O = make_float2(0.f, 0.f);  // FP16 frame offsets (fwd, rev)
+      if (resume) {
+        const int64_t c0 = x + (int64_t)lane * SH;
+        if constexpr (PREC == 0) {
+          if constexpr (ST16) {
+            // FP16 row state: half2 cells relative to the offset of their
+            // 512-column group (the saving strip's frame); re-based onto this
+            // strip's minimum
+            const uint4 *hc = reinterpret_cast<const uint4 *>(reinterpret_cast<const __half2 *>(st_plane0) + c0);
+            const float2 *og = reinterpret_cast<const float2 *>(st_plane0 + p.m_pad);
   #pragma unroll
             for (int k = 0; k < SH / 4; ++k) {
-              const float4 u = f0[k], v = f1[k];
-              mx = fminf(mx, fminf(fminf(u.x, u.y), fminf(u.z, u.w)));
-              my = fminf(my, fminf(fminf(v.x, v.y), fminf(v.z, v.w)));
+              const uint4 u = hc[k];
+              D[4 * k] = bits_as<__half2>(u.x);
+              D[4 * k + 1] = bits_as<__half2>(u.y);
+              D[4 * k + 2] = bits_as<__half2>(u.z);
+              D[4 * k + 3] = bits_as<__half2>(u.w);
+            }
+            float mx = __int_as_float(0x7f800000), my = mx;
+  #pragma unroll
+            for (int k = 0; k < SH; ++k) {
+              const float2 o = og[(c0 + k) >> 9];
+              const float2 v = __half22float2(D[k]);
+              mx = fminf(mx, v.x + o.x);
+              my = fminf(my, v.y + o.y);
             }
   #pragma unroll
             for (int m = 16; m >= 1; m >>= 1) {
@@ -663,175 +637,198 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
             }
             O = make_float2(mx, my);
   #pragma unroll
-            for (int k = 0; k < SH / 4; ++k) {
-              const float4 u = f0[k], v = f1[k];
-              D[4 * k] = __floats2half2_rn(u.x - mx, v.x - my);
-              D[4 * k + 1] = __floats2half2_rn(u.y - mx, v.y - my);
-              D[4 * k + 2] = __floats2half2_rn(u.z - mx, v.z - my);
-              D[4 * k + 3] = __floats2half2_rn(u.w - mx, v.w - my);
-            }
+            for (int k = 0; k < SH; ++k) {
+              const float2 o = og[(c0 + k) >> 9];
+              const float2 v = __half22float2(D[k]);
+              D[k] = __floats2half2_rn(v.x + o.x - mx, v.y + o.y - my);
             }
           } else {
-            const float4 *f = reinterpret_cast<const float4 *>(st_plane0 + (int64_t)strand * p.m_pad + c0);
+          // two passes over the saved planes: strip minimum first, then the cells
+          const float4 *f0 = reinterpret_cast<const float4 *>(st_plane0 + c0);
+          const float4 *f1 = reinterpret_cast<const float4 *>(st_plane0 + p.m_pad + c0);
+          float mx = __int_as_float(0x7f800000), my = mx;
   #pragma unroll
-            for (int k = 0; k < SH / 4; ++k) {
-              const float4 u = f[k];
-              D[4 * k] = u.x;
-              D[4 * k + 1] = u.y;
-              D[4 * k + 2] = u.z;
-              D[4 * k + 3] = u.w;
-            }
+          for (int k = 0; k < SH / 4; ++k) {
+            const float4 u = f0[k], v = f1[k];
+            mx = fminf(mx, fminf(fminf(u.x, u.y), fminf(u.z, u.w)));
+            my = fminf(my, fminf(fminf(v.x, v.y), fminf(v.z, v.w)));
+          }
+  #pragma unroll
+          for (int m = 16; m >= 1; m >>= 1) {
+            mx = fminf(mx, __shfl_xor_sync(FULL_MASK, mx, m));
+            my = fminf(my, __shfl_xor_sync(FULL_MASK, my, m));
+          }
+          O = make_float2(mx, my);
+  #pragma unroll
+          for (int k = 0; k < SH / 4; ++k) {
+            const float4 u = f0[k], v = f1[k];
+            D[4 * k] = __floats2half2_rn(u.x - mx, v.x - my);
+            D[4 * k + 1] = __floats2half2_rn(u.y - mx, v.y - my);
+            D[4 * k + 2] = __floats2half2_rn(u.z - mx, v.z - my);
+            D[4 * k + 3] = __floats2half2_rn(u.w - mx, v.w - my);
+          }
           }
         } else {
+          const float4 *f = reinterpret_cast<const float4 *>(st_plane0 + (int64_t)strand * p.m_pad + c0);
   #pragma unroll
-          for (int k = 0; k < SH; ++k) D[k] = P::zero();
-        }
-
-        // -- reference strip into registers (after the row state: fewer live registers)
-        RV R[NWH];
-        if (p.use_tma) {
-          const int sl = s & 1;
-          // every lane waits (acquire of the TMA bytes); the give-up decision is warp-uniform
-          const bool ok = __all_sync(FULL_MASK, mbar_wait(&bars[sl], (phase >> sl) & 1u));
-          if (!ok) {
-            atomicOr(p.err, kErrTmaTimeout);  // every lane: same bit
-            return false;
-          }
-          phase ^= 1u << sl;
-          regs_from_smem<NWH, RV>(slot0 + sl * STRIP_BYTES, lane, R);
-          __syncwarp();
-          if (s + 1 < nstrips) {
-            const int ns = (s + 1) & 1;
-            fence_proxy_async_smem();
-            tma_issue_if(slot0 + ns * STRIP_BYTES, &tmap, &bars[ns], 0,
-                         (int)((ref_plane + (s + 1 < nh ? x + WH : a)) * RB / 128),
-                         STRIP_BYTES, is0);
-          }
-        } else if constexpr (PREC == 1) {
-          if (p.ref_layout == 0)
-            regs_from_pairs<SH>(reinterpret_cast<const float2 *>(p.ref_plain), x, lane, strand, R);
-          else
-            regs_from_global<NWH, RV>(reinterpret_cast<const float *>(p.ref_plain) + ref_plane + x, lane, R);
-        } else if constexpr (PREC == 2) {
-          regs_from_global<NWH, RV>(reinterpret_cast<const __half *>(p.ref_plain) + ref_plane + x, lane, R);
-        } else {
-          regs_from_global<NWH, RV>(reinterpret_cast<const __half2 *>(p.ref_plain) + x, lane, R);
-        }
-
-        // uniform stores (every lane writes the same value): no lane-dependent branch
-        seam_out[0] = P::shfl(D[SH - 1], 31);
-        if constexpr (PREC == 0) off_out[0] = O;
-
-        // offset of this strip's frame relative to the left strip's frame (FP16)
-        V delta = P::zero();
-        float2 off_next = make_float2(0.f, 0.f);
-        if constexpr (PREC == 0) {
-          if (!first) {
-            const float2 oi = off_in[0];
-            delta = __float22half2_rn(make_float2(oi.x - O.x, oi.y - O.y));
-            if (n >= K) off_next = off_in[1];
+          for (int k = 0; k < SH / 4; ++k) {
+            const float4 u = f[k];
+            D[4 * k] = u.x;
+            D[4 * k + 1] = u.y;
+            D[4 * k + 2] = u.z;
+            D[4 * k + 3] = u.w;
           }
         }
-
-        // -- row sweep, 32 rows per window: lane l holds query sample i0+l and
-        // the incoming seam value of row i0+l, already re-based into this strip's
-        // frame (delta changes only at a rescale, which ends a window)
-        const V vinf = P::inf();
-        typename P::QW qwin = P::qw(lane < n ? q[lane] : 0.f);
-        // REF_DEL also reads the seam value of the last row itself (one entry further)
-        constexpr int kExtra = RD ? 1 : 0;
-        V swin = (!first && lane < rows + kExtra) ? seam_in[lane] : vinf;
-        if constexpr (PREC == 0) swin = __hadd2(swin, delta);
-        V *so = seam_out + 1;  // seam value of row i goes to seam_out[i + 1]
-        for (int i0 = 0; i0 < rows; i0 += kWarp) {
-          const int r = i0 + kWarp + lane;
-          const float qn = r < n ? q[r] : 0.f;
-          const V sn = (!first && r < rows + kExtra) ? seam_in[r] : vinf;
-          // the seam column leaving this strip is gathered in a register window
-          // (lane l keeps row i0+l) and stored once per 32 rows, coalesced: no
-          // lane-conditional store inside the row loop
-          V sout = vinf;
-          // REF_DEL: lane l of lwin holds the left strip's value on row i0+l itself
-          V lwin = vinf;
-          if constexpr (RD) {
-            V last = P::shfl(sn, 0);  // the left strip's value on row i0+31, stored after its rescale
-            if constexpr (PREC == 0) {
-              // that value is in the left strip's next frame: re-base with the next epoch's offset
-              last = __hadd2(last, __float22half2_rn(make_float2(off_next.x - O.x, off_next.y - O.y)));
-            }
-            lwin = P::sel(lane == kWarp - 1, last, __shfl_down_sync(FULL_MASK, swin, 1));
-          }
-          if (rows - i0 >= kWarp) {
-  #pragma unroll 4
-            for (int il = 0; il < kWarp; ++il) {
-              if constexpr (RD)
-                row_refdel<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
-              else
-                row<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
-              if constexpr (SMEM_SEAM)
-                st_shared_if(sob + 4u * (uint32_t)il, cell_bits<PREC>(D[SH - 1]), is31);
-              else
-                sout = P::sel(lane == il, P::shfl(D[SH - 1], 31), sout);
-            }
-            if constexpr (PREC == 0) {
-              // rescale: subtract this strip's row minimum (one epoch = 32 rows)
-              V mn = D[0];
+      } else {
   #pragma unroll
-              for (int k = 1; k < SH; ++k) mn = __hmin2(mn, D[k]);
-  #pragma unroll
-              for (int m = 16; m >= 1; m >>= 1) mn = __hmin2(mn, P::shfl_xor(mn, m));
-  #pragma unroll
-              for (int k = 0; k < SH; ++k) D[k] = __hsub2(D[k], mn);
-              const float2 mf = __half22float2(mn);
-              O.x += mf.x;
-              O.y += mf.y;
-              const int e = (i0 + kWarp) / K;
-              off_out[e] = O;  // warp-uniform value, stored by every lane
-              sout = P::sel(lane == kWarp - 1, P::shfl(D[SH - 1], 31), sout);  // the seam leaves in the new frame
-              if (!first) {
-                delta = __float22half2_rn(make_float2(off_next.x - O.x, off_next.y - O.y));
-                if ((e + 1) * K <= n) off_next = off_in[e + 1];
-              }
-            }
-            if constexpr (SMEM_SEAM) {
-              __syncwarp();
-              sout = P::from_bits(ld_shared_u32(sob + 4u * (uint32_t)lane));
-              __syncwarp();
-            }
-            so[lane] = sout;
-          } else {
-            const int cnt = rows - i0;
-            for (int il = 0; il < cnt; ++il) {
-              if constexpr (RD)
-                row_refdel<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
-              else
-                row<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
-              if constexpr (SMEM_SEAM)
-                st_shared_if(sob + 4u * (uint32_t)il, cell_bits<PREC>(D[SH - 1]), is31);
-              else
-                sout = P::sel(lane == il, P::shfl(D[SH - 1], 31), sout);
-            }
-            if constexpr (SMEM_SEAM) {
-              __syncwarp();
-              sout = lane < cnt ? P::from_bits(ld_shared_u32(sob + 4u * (uint32_t)lane)) : vinf;
-              __syncwarp();
-            }
-            so[lane] = sout;  // lanes >= cnt write +inf into the buffer's 32-entry slack past the rows
-          }
-          so += kWarp;
-          qwin = P::qw(qn);
-          swin = sn;
-          if constexpr (PREC == 0) swin = __hadd2(swin, delta);
+        for (int k = 0; k < SH; ++k) D[k] = P::zero();
+      }
+
+      // -- reference strip into registers (after the row state: fewer live registers)
+      RV R[NWH];
+      if (p.use_tma) {
+        const int sl = s & 1;
+        // every lane waits (acquire of the TMA bytes); the give-up decision is warp-uniform
+        const bool ok = __all_sync(FULL_MASK, mbar_wait(&bars[sl], (phase >> sl) & 1u));
+        if (!ok) {
+          atomicOr(p.err, kErrTmaTimeout);  // every lane: same bit
+          return false;
         }
-        if (rows < n) {
-          // rows this halo strip skipped can no longer reach column a: keep them
-          // inert (whole 32-entry groups; the buffers have 32 entries of slack)
-          for (int rr = rows + 1; rr <= n; rr += kWarp) seam_out[rr + lane] = vinf;
-          if constexpr (PREC == 0) {
-            for (int e = rows / K + 1; e <= n / K; e += kWarp) off_out[e + lane] = O;
-          }
-        }
+        phase ^= 1u << sl;
+        regs_from_smem<NWH, RV>(slot0 + sl * STRIP_BYTES, lane, R);
         __syncwarp();
+        if (s + 1 < nstrips) {
+          const int ns = (s + 1) & 1;
+          fence_proxy_async_smem();
+          tma_issue_if(slot0 + ns * STRIP_BYTES, &tmap, &bars[ns], 0,
+                       (int)((ref_plane + (s + 1 < nh ? x + WH : a)) * RB / 128),
+                       STRIP_BYTES, is0);
+        }
+      } else if constexpr (PREC == 1) {
+        if (p.ref_layout == 0)
+          regs_from_pairs<SH>(reinterpret_cast<const float2 *>(p.ref_plain), x, lane, strand, R);
+        else
+          regs_from_global<NWH, RV>(reinterpret_cast<const float *>(p.ref_plain) + ref_plane + x, lane, R);
+      } else if constexpr (PREC == 2) {
+        regs_from_global<NWH, RV>(reinterpret_cast<const __half *>(p.ref_plain) + ref_plane + x, lane, R);
+      } else {
+        regs_from_global<NWH, RV>(reinterpret_cast<const __half2 *>(p.ref_plain) + x, lane, R);
+      }
+
+      // uniform stores (every lane writes the same value): no lane-dependent branch
+      seam_out[0] = P::shfl(D[SH - 1], 31);
+      if constexpr (PREC == 0) off_out[0] = O;
+
+      // offset of this strip's frame relative to the left strip's frame (FP16)
+      V delta = P::zero();
+      float2 off_next = make_float2(0.f, 0.f);
+      if constexpr (PREC == 0) {
+        if (!first) {
+          const float2 oi = off_in[0];
+          delta = __float22half2_rn(make_float2(oi.x - O.x, oi.y - O.y));
+          if (n >= K) off_next = off_in[1];
+        }
+      }
+
+      // -- row sweep, 32 rows per window: lane l holds query sample i0+l and
+      // the incoming seam value of row i0+l, already re-based into this strip's
+      // frame (delta changes only at a rescale, which ends a window)
+      const V vinf = P::inf();
+      typename P::QW qwin = P::qw(lane < n ? q[lane] : 0.f);
+      // REF_DEL also reads the seam value of the last row itself (one entry further)
+      constexpr int kExtra = RD ? 1 : 0;
+      V swin = (!first && lane < rows + kExtra) ? seam_in[lane] : vinf;
+      if constexpr (PREC == 0) swin = __hadd2(swin, delta);
+      V *so = seam_out + 1;  // seam value of row i goes to seam_out[i + 1]
+      for (int i0 = 0; i0 < rows; i0 += kWarp) {
+        const int r = i0 + kWarp + lane;
+        const float qn = r < n ? q[r] : 0.f;
+        const V sn = (!first && r < rows + kExtra) ? seam_in[r] : vinf;
+        // the seam column leaving this strip is gathered in a register window
+        // (lane l keeps row i0+l) and stored once per 32 rows, coalesced: no
+        // lane-conditional store inside the row loop
+        V sout = vinf;
+        // REF_DEL: lane l of lwin holds the left strip's value on row i0+l itself
+        V lwin = vinf;
+        if constexpr (RD) {
+          V last = P::shfl(sn, 0);  // the left strip's value on row i0+31, stored after its rescale
+          if constexpr (PREC == 0) {
+            // that value is in the left strip's next frame: re-base with the next epoch's offset
+            last = __hadd2(last, __float22half2_rn(make_float2(off_next.x - O.x, off_next.y - O.y)));
+          }
+          lwin = P::sel(lane == kWarp - 1, last, __shfl_down_sync(FULL_MASK, swin, 1));
+        }
+        if (rows - i0 >= kWarp) {
+  #pragma unroll 4
+          for (int il = 0; il < kWarp; ++il) {
+            if constexpr (RD)
+              row_refdel<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
+            else
+              row<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+            if constexpr (SMEM_SEAM)
+              st_shared_if(sob + 4u * (uint32_t)il, cell_bits<PREC>(D[SH - 1]), is31);
+            else
+              sout = P::sel(lane == il, P::shfl(D[SH - 1], 31), sout);
+          }
+          if constexpr (PREC == 0) {
+            // rescale: subtract this strip's row minimum (one epoch = 32 rows)
+            V mn = D[0];
+  #pragma unroll
+            for (int k = 1; k < SH; ++k) mn = __hmin2(mn, D[k]);
+  #pragma unroll
+            for (int m = 16; m >= 1; m >>= 1) mn = __hmin2(mn, P::shfl_xor(mn, m));
+  #pragma unroll
+            for (int k = 0; k < SH; ++k) D[k] = __hsub2(D[k], mn);
+            const float2 mf = __half22float2(mn);
+            O.x += mf.x;
+            O.y += mf.y;
+            const int e = (i0 + kWarp) / K;
+            off_out[e] = O;  // warp-uniform value, stored by every lane
+            sout = P::sel(lane == kWarp - 1, P::shfl(D[SH - 1], 31), sout);  // the seam leaves in the new frame
+            if (!first) {
+              delta = __float22half2_rn(make_float2(off_next.x - O.x, off_next.y - O.y));
+              if ((e + 1) * K <= n) off_next = off_in[e + 1];
+            }
+          }
+          if constexpr (SMEM_SEAM) {
+            __syncwarp();
+            sout = P::from_bits(ld_shared_u32(sob + 4u * (uint32_t)lane));
+            __syncwarp();
+          }
+          so[lane] = sout;
+        } else {
+          const int cnt = rows - i0;
+          for (int il = 0; il < cnt; ++il) {
+            if constexpr (RD)
+              row_refdel<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
+            else
+              row<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+            if constexpr (SMEM_SEAM)
+              st_shared_if(sob + 4u * (uint32_t)il, cell_bits<PREC>(D[SH - 1]), is31);
+            else
+              sout = P::sel(lane == il, P::shfl(D[SH - 1], 31), sout);
+          }
+          if constexpr (SMEM_SEAM) {
+            __syncwarp();
+            sout = lane < cnt ? P::from_bits(ld_shared_u32(sob + 4u * (uint32_t)lane)) : vinf;
+            __syncwarp();
+          }
+          so[lane] = sout;  // lanes >= cnt write +inf into the buffer's 32-entry slack past the rows
+        }
+        so += kWarp;
+        qwin = P::qw(qn);
+        swin = sn;
+        if constexpr (PREC == 0) swin = __hadd2(swin, delta);
+      }
+      if (rows < n) {
+        // rows this halo strip skipped can no longer reach column a: keep them
+        // inert (whole 32-entry groups; the buffers have 32 entries of slack)
+        for (int rr = rows + 1; rr <= n; rr += kWarp) seam_out[rr + lane] = vinf;
+        if constexpr (PREC == 0) {
+          for (int e = rows / K + 1; e <= n / K; e += kWarp) off_out[e + lane] = O;
+        }
+      }
+      __syncwarp();
 
       return true;
     };
