@@ -219,15 +219,19 @@ def run_serving(name: str, precision: int, device: int, duration_s: float, batch
 
 
 REF_GPU_GEOMETRY = {"C2": "fp16_1000064"}
+REF_GPU_GEOMETRY_FP32 = {"C2": "fp32_2000128"}
 
 
-def reference_gpu_kernel(workload, n_reads: int = 2048, shipped_launches: int = 2):
+def reference_gpu_kernel(workload, n_reads: int = 2048, shipped_launches: int = 2, fp32_reads: int = 4):
     """The reference's own FP16 kernel (FullDTW::DTW, src/include/DTW.cu,
     compiled from its sources into oracle/_ref) on this GPU, on the workload's
     genome: reads of the kernel's fixed 2,048-sample query from the same
     generator, levels from the oracle's restatement of the reference's builder.
     Two launch patterns: main.cu's (BLOCK_NUM = 10 reads per launch, one
     stream, `shipped_launches` launches timed) and every read in one launch.
+    Beside it the reference's FP32 build of the same kernel (strands
+    concatenated, load_reference.hpp:36-37) with one read per launch: the
+    plain one-read-per-launch FP32 sDTW, timed on `fp32_reads` reads.
     Returns the record, or {"unavailable": why}."""
     import torch
     from dtwax_gb300 import synth
@@ -283,6 +287,32 @@ def reference_gpu_kernel(workload, n_reads: int = 2048, shipped_launches: int = 
         ms = b.elapsed_time(e)
         out["one_launch"] = {"value": n_reads * cells_per_read / (ms * 1e-3) / 1e9,
                              "reads_per_s": n_reads / (ms * 1e-3), "ms": ms, "reads": n_reads}
+    name32 = REF_GPU_GEOMETRY_FP32.get(workload.name)
+    if name32 is None or not RK.available(name32):
+        out["fp32_one_read_per_launch"] = {"unavailable": f"no FP32 reference-kernel cubin for {workload.name}"}
+        return out
+    with RK.RefKernel(name32) as k:
+        d_ref = k.reference(fwd.astype(np.float32), rev.astype(np.float32))
+        d_q = k.queries(z[:fp32_reads])
+        d_dist = torch.empty(fp32_reads, dtype=torch.float32, device="cuda")
+        d_last = torch.empty(k.ref_len, dtype=torch.float32, device="cuda")
+        stream = torch.cuda.current_stream()
+        sh = stream.cuda_stream
+        k.launch(d_ref, d_q, d_dist, d_last, 1, stream=sh)  # warm-up
+        torch.cuda.synchronize()
+        b, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        b.record(stream)
+        for i in range(fp32_reads):
+            k.launch(d_ref, d_q, d_dist[i:], d_last, 1, first_read=i, stream=sh)
+        e.record(stream)
+        torch.cuda.synchronize()
+        ms = b.elapsed_time(e)
+        out["fp32_one_read_per_launch"] = {
+            "kernel": f"FullDTW::DTW<int, float> (-DNO_REF_DEL), cubin {name32}: fwd and rev concatenated, "
+                      f"{-(-2 * m // RK.TILE)} tiles",
+            "value": fp32_reads * cells_per_read / (ms * 1e-3) / 1e9, "reads_per_s": fp32_reads / (ms * 1e-3),
+            "ms": ms, "reads": fp32_reads, "launches": fp32_reads,
+            "score_min": float(d_dist.min().item()), "score_max": float(d_dist.max().item())}
     return out
 
 

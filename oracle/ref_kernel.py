@@ -61,6 +61,7 @@ GEOMETRIES = {
     "fp16_1000064": ("fp16", 1000064, False),    # 1,202 tiles: a 1 Mb genome (999,995 columns per strand)
     "fp32_8320": ("fp32", 8320, False),          # 2 x 4,160 concatenated
     "fp32_94848": ("fp32", 94848, False),        # 2 x 47,424 concatenated (114 tiles)
+    "fp32_2000128": ("fp32", 2000128, False),    # 2 x 1,000,064 concatenated: a 1 Mb genome (2,404 tiles)
     "fp16_4160_rd": ("fp16", 4160, True),
     "fp16_48128_rd": ("fp16", 48128, True),
     "fp32_8320_rd": ("fp32", 8320, True),

@@ -95,6 +95,31 @@ def test_refkernel_fp32_matches_model(small, oracle):
         assert (rel(got[nz:nz + len(crafted)], without) > 0.1).any(), bit
 
 
+def test_refkernel_fp32_at_the_1mb_geometry(built_lib, oracle):
+    """The FP32 geometry the benchmark's reference arm times one read per
+    launch (a 1 Mb genome, fwd and rev concatenated, 2,404 tiles) computes the
+    kernel's recurrence there too: a target and a non-target read, each in its
+    own launch, against the FP64 model within 1e-5."""
+    need("fp32_2000128")
+    g = synth.random_genome(1_000_000, 1)
+    o = synth.random_genome(1_000_000, 2)
+    table = synth.level_table()
+    with make_classifier(g, table, precision=1) as clf:
+        fwd, rev = clf.reference()
+    reads = synth.simulate_reads(g, o, table, [QLEN] * 2, np.array([1, 0], np.int8), seed=5)
+    z = zscore_reads(oracle, reads)
+    with RK.RefKernel("fp32_2000128") as k:
+        got = k.run(k.reference(fwd, rev), z, reads_per_launch=1)
+        half = k.ref_len // 2
+    cat = np.full(2 * half, np.inf)
+    cat[: fwd.size] = fwd
+    cat[half: half + rev.size] = rev
+    model = oracle.sdtw_refkernel_batch(cat, z.astype(np.float64), oracle.REFK_ALL)
+    print(f"\nFP32 reference kernel, 1 Mb geometry: scores {got}, max rel vs model {rel(got, model).max():.2e}")
+    assert rel(got, model).max() <= 1e-5
+    assert got[0] < got[1]  # the target read scores lower
+
+
 def test_refkernel_fp16_matches_model(small, oracle):
     need("fp16_4160")
     fwd, rev, z, crafted, _ = small
