@@ -103,6 +103,27 @@ def test_resume_fp16_state_matches_oracle(setup, oracle):
                 assert dd["score"] == pytest.approx(s, rel=1e-2)
 
 
+@pytest.mark.parametrize("state", ["fp32", "fp16"])
+def test_resume_narrow_halo_matches_oracle(setup, oracle, state):
+    """Chunks of 3 strips run the kernel instance with 16-cell halo strips,
+    for both row-state layouts: resumed decisions stay within the FP16
+    tolerance of the FP64 oracle."""
+    import dtwax_gb300 as d
+    g, o, tab, reads = setup
+    sp = d.STATE_FP16 if state == "fp16" else d.STATE_FP32
+    with make_classifier(g, tab, precision=d.FP16, state_precision=sp, threshold=-1.0, cells_per_thread=48,
+                         chunk_strips=3) as clf:
+        fwd, rev = clf.reference()
+        chunks = {i: split(reads.read(i), 1600) for i in range(reads.n)}
+        got = serve_reads(clf, chunks, chunks_per_decision=3)
+        t = clf.tuning()
+    assert t["narrow_halo"] == 1 and t["chunk_strips"] == 3
+    for i in range(reads.n):
+        want = oracle_decisions(oracle, fwd.astype(np.float64), rev.astype(np.float64), chunks[i][:3])
+        for dd, (sc, e, st) in zip(got[i], want):
+            assert dd["score"] == pytest.approx(sc, rel=1e-2)
+
+
 def test_int16_chunks_match_float_chunks(setup):
     """Raw int16 ADC chunks with their scaling give the decisions of the same
     chunks converted to pA on the host."""
