@@ -13,6 +13,11 @@ carries one read at a time, a new read starts after an exponential gap (mean
 Reads come from a pool of seeded synthetic squiggles (targets from the target
 genome, others from a second genome).  Latency is measured from the scheduled
 arrival of a read's last needed chunk to its decision.
+
+`ReadUntilClientSource` takes the chunks from a live Read Until client instead
+(the read_until package's ReadUntilClient), and its decisions drive the
+client: non-target reads are ejected with unblock_read, and no more data is
+requested for any decided read.
 """
 from __future__ import annotations
 
@@ -108,7 +113,10 @@ class SimulatedSequencer:
                 heapq.heappush(self.events, (t + cfg.period_s + self.rng.exponential(1.0 / cfg.read_rate), ch, g))
         return out
 
-    def decided(self, ch: int, rn: int, now_s: float):
+    def reads_started(self) -> int:
+        return self.next_read - 1
+
+    def decided(self, ch: int, rn: int, now_s: float, call: int = -1):
         """The library decided read rn: the sequencer stops sending its chunks
         (ejected, or no more chunks needed) and the channel starts a new read
         after an exponential gap."""
@@ -117,6 +125,85 @@ class SimulatedSequencer:
             self.active.pop(ch)
             self.gen[ch] += 1  # the channel's pending chunk event is dropped
             heapq.heappush(self.events, (now_s + self.rng.exponential(1.0 / self.cfg.read_rate), ch, self.gen[ch]))
+
+
+class ReadUntilClientSource:
+    """Chunks from a live Read Until client, in place of the reference's FIFO
+    bridge (src/ReadUntil/ont_readuntil.py:29-59, which pipes raw chunks to
+    src/ru_main.cu and ejects every read it sees).
+
+    `client` follows the read_until package's ReadUntilClient
+    (read_until/base.py:344-378): `is_running`, `get_read_chunks(batch_size,
+    last)` yielding (channel, read) with `read.number` and `read.raw_data`,
+    `signal_dtype`, `unblock_read(channel, read_number, duration)` and
+    `stop_receiving_read(channel, read_number)`.  Calibrated (float) signal is
+    used as it comes; integer ADC signal needs `calibration(channel) ->
+    (offset, range, digitisation)` and is scaled to pA as
+    (raw + offset) * range / digitisation.
+
+    The library's decision drives the client:
+    * a target keeps sequencing and gets stop_receiving_read;
+    * a non-target (early or final) gets unblock_read, then
+      stop_receiving_read.
+    Chunks of a decided read that were already queued are dropped.  A read's
+    `max_chunks`-th chunk is marked last, so the library decides it there."""
+
+    def __init__(self, client, batch_size: int = 512, max_chunks: int = 3, unblock_duration: float = 0.1,
+                 calibration=None):
+        self.client = client
+        self.batch_size = batch_size
+        self.max_chunks = max_chunks
+        self.unblock_duration = unblock_duration
+        self.calibration = calibration
+        self.seen = {}        # (channel, read_number) -> chunks submitted
+        self.done = set()     # decided (channel, read_number)
+        self.truth = {}       # unknown for live reads
+        self.started = 0
+        self.actions = {"unblock": 0, "stop": 0}
+
+    def reads_started(self) -> int:
+        return self.started
+
+    def _samples(self, channel, read) -> np.ndarray:
+        dt = np.dtype(self.client.signal_dtype)
+        x = np.frombuffer(read.raw_data, dt)
+        if dt.kind in "iu":
+            if self.calibration is None:
+                raise ValueError("integer signal needs calibration(channel) -> (offset, range, digitisation)")
+            off, rng_, digi = self.calibration(channel)
+            return ((x.astype(np.float32) + np.float32(off)) * np.float32(rng_ / digi)).astype(np.float32)
+        return x.astype(np.float32, copy=False)
+
+    def due(self, now_s: float):
+        out = []
+        if not self.client.is_running:
+            return out
+        for channel, read in self.client.get_read_chunks(batch_size=self.batch_size, last=True):
+            key = (channel, read.number)
+            if key in self.done:
+                continue
+            k = self.seen.get(key, 0)
+            if k >= self.max_chunks:
+                continue
+            if k == 0:
+                self.started += 1
+            self.seen[key] = k + 1
+            x = self._samples(channel, read)
+            if x.size:
+                out.append((now_s, channel, read.number, x, k + 1 >= self.max_chunks))
+        return out
+
+    def decided(self, ch: int, rn: int, now_s: float, call: int = -1):
+        key = (ch, rn)
+        if key in self.done:
+            return
+        self.done.add(key)
+        self.seen.pop(key, None)
+        if call != 1:
+            self.client.unblock_read(ch, rn, duration=self.unblock_duration)
+            self.actions["unblock"] += 1
+        self.client.stop_receiving_read(ch, rn)
+        self.actions["stop"] += 1
 
 
 def run(clf, reads, cfg: ServeConfig, accept: float, reject: float, state_budget_bytes: float = 0.0,
@@ -167,7 +254,7 @@ def _loop(clf, seq, cfg: ServeConfig, drain: bool) -> dict:
         clf.serve_step()
         for d in clf.poll_decisions(8192):
             if d["decided"]:
-                seq.decided(d["channel"], d["read_number"], now_s)
+                seq.decided(d["channel"], d["read_number"], now_s, d["call"])
                 if now_s >= cfg.warmup_s:
                     decided_in_window += 1
                     lat.append(d["latency_ms"])
@@ -182,7 +269,8 @@ def _loop(clf, seq, cfg: ServeConfig, drain: bool) -> dict:
     queue = np.asarray(queue)
     calls = np.asarray(calls)
     truth = np.asarray(truth)
-    acc = float((calls == truth).mean()) if calls.size else float("nan")
+    known = truth >= 0  # reads of a live client have no ground truth
+    acc = float((calls[known] == truth[known]).mean()) if known.any() else float("nan")
     return {
         "channels": cfg.channels, "chunk_samples": cfg.chunk, "duration_s": cfg.duration_s,
         "reads_per_s": decided_in_window / cfg.duration_s,
@@ -200,8 +288,8 @@ def _loop(clf, seq, cfg: ServeConfig, drain: bool) -> dict:
         "mean_batch_reads": st["mean_batch_reads"], "batches": st["batches"],
         "mean_batch_ms": st["mean_batch_ms"], "max_batch_ms": st["max_batch_ms"],
         "reads_deferred": st["reads_deferred"], "max_in_flight": st["max_in_flight"],
-        "reads_started": seq.next_read - 1,
-        "deferred_fraction": st["reads_deferred"] / max(seq.next_read - 1, 1),
+        "reads_started": seq.reads_started(),
+        "deferred_fraction": st["reads_deferred"] / max(seq.reads_started(), 1),
         "queue_depth_end": st["queue_depth"],
         "state_bytes": st["state_bytes"],
     }

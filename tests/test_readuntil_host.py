@@ -1,7 +1,9 @@
 """CPU tests of the Read Until loop (dtwax_gb300/readuntil.py) against a fake
-serving library: chunk flow, decisions, latency bookkeeping and the
-simulated sequencer's channel handling."""
+serving library: chunk flow, decisions, latency bookkeeping, the simulated
+sequencer's channel handling, and a fake live Read Until client whose
+unblock / stop actions the decisions drive."""
 import numpy as np
+import pytest
 
 from dtwax_gb300 import readuntil, synth
 
@@ -80,3 +82,78 @@ def test_sequencer_drops_chunks_of_decided_reads():
         ks = [x for x in later if x[1] == c and x[2] == r]
         assert len(ks) == cfg.chunks_per_read - 1 and ks[-1][4]
     assert np.isfinite([t for t, _, _, _, _ in later]).all()
+
+
+class FakeRead:
+    def __init__(self, number, data):
+        self.number = number
+        self.id = f"read-{number}"
+        self.raw_data = data.tobytes()
+
+
+class FakeClient:
+    """The read_until ReadUntilClient surface the loop uses: chunks arrive in
+    rounds (every read's first chunk, then every read's second, ...), one
+    round per get_read_chunks call; actions are recorded."""
+
+    def __init__(self, rounds, dtype):
+        self.rounds = rounds
+        self.signal_dtype = dtype
+        self.unblocked, self.stopped = [], []
+
+    @property
+    def is_running(self):
+        return bool(self.rounds)
+
+    def get_read_chunks(self, batch_size=1, last=True):
+        return self.rounds.pop(0)[:batch_size] if self.rounds else []
+
+    def unblock_read(self, read_channel, read_number, duration=0.1):
+        self.unblocked.append((read_channel, read_number))
+
+    def stop_receiving_read(self, read_channel, read_number):
+        self.stopped.append((read_channel, read_number))
+
+
+class RecordingServer(FakeServer):
+    def __init__(self, truth):
+        super().__init__(truth)
+        self.samples = {}
+
+    def submit_chunk(self, ch, rn, x, is_last=False, arrival_ms=-1.0):
+        self.samples.setdefault(rn, []).append(np.array(x, copy=True))
+        super().submit_chunk(ch, rn, x, is_last, arrival_ms)
+
+
+def test_live_client_decisions_drive_unblock():
+    """Reads 1-6 on channels 1-6, three chunks each; the library decides each
+    read on its first chunk.  Non-targets (odd read numbers) are ejected,
+    every decided read stops receiving data, and later chunks of decided reads
+    never reach the library."""
+    rng = np.random.default_rng(0)
+    chunks = {rn: [rng.normal(90, 10, 400).astype(np.float32) for _ in range(3)] for rn in range(1, 7)}
+    rounds = [[(rn, FakeRead(rn, chunks[rn][k])) for rn in range(1, 7)] for k in range(3)]
+    client = FakeClient(rounds, np.float32)
+    src = readuntil.ReadUntilClientSource(client, batch_size=16, max_chunks=3)
+    srv = RecordingServer(lambda rn: rn % 2 == 0)
+    cfg = readuntil.ServeConfig(channels=6, chunk=400, duration_s=0.3, warmup_s=0.0)
+    rec = readuntil.run(srv, None, cfg, accept=0.1, reject=0.2, sequencer=src)
+    assert sorted(client.unblocked) == [(rn, rn) for rn in (1, 3, 5)]
+    assert sorted(client.stopped) == [(rn, rn) for rn in range(1, 7)]
+    assert src.reads_started() == 6 and rec["reads_started"] == 6
+    for rn in range(1, 7):
+        assert len(srv.samples[rn]) == 1  # decided on its first chunk
+        np.testing.assert_array_equal(srv.samples[rn][0], chunks[rn][0])
+    assert np.isnan(rec["call_accuracy"])  # live reads carry no ground truth
+
+
+def test_live_client_int16_signal_is_calibrated():
+    raw = (np.arange(400) % 50 - 10).astype(np.int16)
+    client = FakeClient([[(3, FakeRead(9, raw))]], np.int16)
+    src = readuntil.ReadUntilClientSource(client, max_chunks=1, calibration=lambda ch: (12.0, 1400.0, 8192.0))
+    (t, ch, rn, x, last), = src.due(0.0)
+    assert (ch, rn, last) == (3, 9, True)
+    np.testing.assert_allclose(x, (raw.astype(np.float32) + 12.0) * np.float32(1400.0 / 8192.0), rtol=1e-6)
+    src_nocal = readuntil.ReadUntilClientSource(FakeClient([[(3, FakeRead(9, raw))]], np.int16))
+    with pytest.raises(ValueError):
+        src_nocal.due(0.0)
