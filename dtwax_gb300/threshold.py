@@ -13,7 +13,13 @@
 * ``call`` is the online decision of src/ReadUntil/plot_realtime.py:42-43
   (score > t -> non-target; the offline tuner counts score == t as
   non-target, which is the rule used here).
-* ``best_f1_threshold`` is the F1-optimal variant of src/test/find_threshold.py.
+* ``f1_threshold`` is the F1 sweep of src/test/find_threshold.py:60-81:
+  1,000 thresholds in linspace(min - 1, max + 1) over both classes; a read is
+  kept when its score <= t; rates are counted against the non-zero scores of
+  each class (np.count_nonzero); F1 = TPR / (TPR + (FNR + FPR) / 2) with
+  those rates; the first maximum wins.  ``f1_main`` is that script's command
+  line (``<32|16> <target> <other>``: FP32 score files, or FP16 .fwd/.rev
+  pairs whose per-read minimum is taken); it also reads the CLI's logs.
 """
 from __future__ import annotations
 
@@ -62,18 +68,59 @@ def best_threshold(target_scores, other_scores, num: int = 100000, plateau: str 
     return float(th[k]), float(acc[k])
 
 
-def best_f1_threshold(target_scores, other_scores, num: int = 100000):
-    """(threshold, F1) with targets as the positive class (score < t)."""
-    t_s = np.sort(np.asarray(target_scores, np.float64))
-    o_s = np.sort(np.asarray(other_scores, np.float64))
-    hi = max(t_s.max(), o_s.max())
-    th = np.linspace(0, hi, num=num)
-    tp = np.searchsorted(t_s, th, side="left").astype(np.float64)
-    fp = np.searchsorted(o_s, th, side="left").astype(np.float64)
-    fn = t_s.size - tp
-    f1 = np.where(tp > 0, 2 * tp / np.maximum(2 * tp + fp + fn, 1), 0.0)
+def f1_threshold(target_scores, other_scores, num: int = 1000) -> dict:
+    """find_threshold.py's sweep.  Returns the best threshold with the rates
+    the script prints: the fraction of targets kept (score <= t), the
+    fraction of others discarded (score > t) and F1; plus the sweep's range
+    and the class means (its first two output lines)."""
+    t_s = np.asarray(target_scores, np.float64)
+    o_s = np.asarray(other_scores, np.float64)
+    if t_s.size == 0 or o_s.size == 0:
+        raise ValueError("both classes need scores")
+    lo = min(t_s.min(), o_s.min()) - 1
+    hi = max(t_s.max(), o_s.max()) + 1
+    th = np.linspace(lo, hi, num=num)
+    ts, os_ = np.sort(t_s), np.sort(o_s)
+    # fraction discarded (score > t), over the non-zero scores of the class
+    vd = (ts.size - np.searchsorted(ts, th, side="right")) / np.count_nonzero(t_s)
+    od = (os_.size - np.searchsorted(os_, th, side="right")) / np.count_nonzero(o_s)
+    f1 = (1 - vd) / ((1 - vd) + 0.5 * (1 + vd - od))
     k = int(np.argmax(f1))
-    return float(th[k]), float(f1[k])
+    return {"threshold": float(th[k]), "target_kept": float(1 - vd[k]), "other_discarded": float(od[k]),
+            "f1": float(f1[k]), "min": float(lo), "max": float(hi), "mean_target": float(t_s.mean()),
+            "mean_other": float(o_s.mean())}
+
+
+def _read_scores(path: str) -> np.ndarray:
+    """One score per line (find_threshold.py's input), or a CLI log."""
+    with open(path) as f:
+        lines = [ln for ln in f.read().splitlines() if ln.strip()]
+    if lines and (len(lines[0].split()) >= 6 or lines[0].split()[0] == "Read_ID"):
+        return parse_log(lines)
+    return np.asarray([float(ln.strip()) for ln in lines], np.float64)
+
+
+def f1_main(argv=None) -> int:
+    """`python -m dtwax_gb300.threshold f1 <32|16> <target> <other>`: the
+    command line and output lines of src/test/find_threshold.py.  With 16 the
+    scores come from <name>.fwd and <name>.rev and a read's score is their
+    minimum; CLI logs (6-column or extended) are read directly."""
+    import sys
+    argv = sys.argv[1:] if argv is None else argv
+    if len(argv) != 3:
+        print("usage: f1 <32|16> <target> <other>")
+        return 2
+    bits, tf, of = int(argv[0]), argv[1], argv[2]
+    if bits == 32:
+        t_s, o_s = _read_scores(tf), _read_scores(of)
+    else:
+        t_s = np.minimum(_read_scores(tf + ".fwd"), _read_scores(tf + ".rev"))
+        o_s = np.minimum(_read_scores(of + ".fwd"), _read_scores(of + ".rev"))
+    r = f1_threshold(t_s, o_s)
+    print(r["min"], r["max"])
+    print(r["mean_target"], r["mean_other"])
+    print(r["target_kept"], r["other_discarded"], r["f1"])
+    return 0
 
 
 def call(scores, threshold: float) -> np.ndarray:
@@ -104,4 +151,7 @@ def main(argv=None) -> int:
 
 
 if __name__ == "__main__":
+    import sys
+    if len(sys.argv) > 1 and sys.argv[1] == "f1":
+        raise SystemExit(f1_main(sys.argv[2:]))
     raise SystemExit(main())

@@ -20,6 +20,10 @@ score_logs.npz
     (targets) and src/unmapped.log (non-targets), plus the threshold and
     accuracy that the reference's own src/ReadUntil/calc_classification_threshold.py
     prints for those two logs (it runs here: it needs numpy only).
+find_threshold.npz
+    The three output lines of the reference's src/test/find_threshold.py
+    (numpy only) on the same two logs: in its FP32 mode on min(fwd, rev) score
+    files, and in its FP16 mode on the .fwd / .rev score-file pairs.
 """
 from __future__ import annotations
 
@@ -115,6 +119,46 @@ def main(ref_root: str) -> None:
         ref_accuracy=np.float64(float(m.group(2))),
     )
     print("threshold", m.group(1), "accuracy", m.group(2), "min", min_score)
+    find_threshold_golden(ref_root)
+
+
+def log_columns(fn):
+    """(fwd, rev) score columns of a 6-column log."""
+    fwd, rev = [], []
+    with open(fn) as f:
+        for line in f:
+            t = line.split()
+            if t[0] == "Read_ID":
+                continue
+            fwd.append(float(t[4]))
+            rev.append(float(t[5]))
+    return np.array(fwd, np.float64), np.array(rev, np.float64)
+
+
+def find_threshold_golden(ref_root: str) -> None:
+    import tempfile
+    script = os.path.join(ref_root, "src/test/find_threshold.py")
+    tf, tr = log_columns(os.path.join(ref_root, "src/mapped.log"))
+    of, orr = log_columns(os.path.join(ref_root, "src/unmapped.log"))
+    rec = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        def write(name, values):
+            with open(os.path.join(tmp, name), "w") as f:
+                f.write("".join(f"{float(v)!r}\n" for v in values))
+        write("t32", np.minimum(tf, tr))
+        write("o32", np.minimum(of, orr))
+        write("t16.fwd", tf)
+        write("t16.rev", tr)
+        write("o16.fwd", of)
+        write("o16.rev", orr)
+        for bits, t, o in (("32", "t32", "o32"), ("16", "t16", "o16")):
+            out = subprocess.run([sys.executable, script, bits, os.path.join(tmp, t), os.path.join(tmp, o)],
+                                 check=True, capture_output=True, text=True, cwd=tmp).stdout
+            vals = [float(x) for line in out.splitlines()[:3] for x in line.split()]
+            rec[f"mode{bits}"] = np.array(vals, np.float64)  # min max, mean_t mean_o, kept discarded f1
+    rec["target_fwd"], rec["target_rev"], rec["other_fwd"], rec["other_rev"] = tf, tr, of, orr
+    np.savez_compressed(os.path.join(HERE, "find_threshold.npz"), **rec)
+    print("find_threshold", rec["mode32"], rec["mode16"])
 
 
 if __name__ == "__main__":

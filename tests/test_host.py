@@ -189,3 +189,41 @@ def test_shard_assignment():
     assert parts[0][0] == 0 and parts[-1][1] == n
     assert all(parts[i][1] == parts[i + 1][0] for i in range(3))
     assert max(b - a for a, b in parts) - min(b - a for a, b in parts) <= 1
+
+
+def test_f1_threshold_matches_find_threshold_py():
+    """The F1 sweep against the output lines of the reference's
+    src/test/find_threshold.py on the reference's FP16 logs (fixture made by
+    tests/golden/make_golden.py)."""
+    from dtwax_gb300 import threshold
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "find_threshold.npz"))
+    r = threshold.f1_threshold(np.minimum(g["target_fwd"], g["target_rev"]),
+                               np.minimum(g["other_fwd"], g["other_rev"]))
+    got = [r["min"], r["max"], r["mean_target"], r["mean_other"], r["target_kept"], r["other_discarded"], r["f1"]]
+    np.testing.assert_allclose(got, g["mode32"], rtol=1e-12)
+    assert r["min"] < r["threshold"] < r["max"]
+
+
+@pytest.mark.parametrize("bits", ["32", "16"])
+def test_f1_command_line(tmp_path, bits):
+    """`python -m dtwax_gb300.threshold f1 <32|16> <target> <other>` prints
+    find_threshold.py's three lines (FP32 score files, or .fwd/.rev pairs)."""
+    import subprocess
+    import sys
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "find_threshold.npz"))
+
+    def write(path, values):
+        path.write_text("".join(f"{float(v)!r}\n" for v in values))
+
+    if bits == "32":
+        write(tmp_path / "t", np.minimum(g["target_fwd"], g["target_rev"]))
+        write(tmp_path / "o", np.minimum(g["other_fwd"], g["other_rev"]))
+    else:
+        for name, key in (("t", "target"), ("o", "other")):
+            write(tmp_path / f"{name}.fwd", g[f"{key}_fwd"])
+            write(tmp_path / f"{name}.rev", g[f"{key}_rev"])
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, "-m", "dtwax_gb300.threshold", "f1", bits, str(tmp_path / "t"),
+                          str(tmp_path / "o")], capture_output=True, text=True, check=True, cwd=root).stdout
+    vals = [float(x) for line in out.splitlines()[:3] for x in line.split()]
+    np.testing.assert_allclose(vals, g[f"mode{bits}"], rtol=1e-12)
