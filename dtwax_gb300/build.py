@@ -21,7 +21,7 @@ LIB = os.path.join(PKG, "libdtwx.so")
 BIN = os.path.join(PKG, "bin", "dtwx_main")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["sdtw.cu", "prep.cu", "api.cpp", "host_util.cpp", "static_scratch.cu"]
+LIB_SOURCES = ["sdtw.cu", "refdel.cu", "prep.cu", "api.cpp", "host_util.cpp", "static_scratch.cu"]
 
 
 def nvcc() -> str:

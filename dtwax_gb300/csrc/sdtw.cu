@@ -36,9 +36,9 @@
 
 #include <cuda/std/cstdint>
 
-namespace dtwx {
+#include "warp_ops.cuh"
 
-#define FULL_MASK 0xffffffffu
+namespace dtwx {
 
 // ---------------------------------------------------------------- precision policies
 // Every policy keeps one 32-bit register per cell so that selects, shuffles
@@ -204,28 +204,10 @@ __device__ __forceinline__ void tma_issue_if(void *dst, const CUtensorMap *map, 
       : "memory");
 }
 
-// Work-queue ticket taken by lane 0 only, broadcast by the caller.
-__device__ __forceinline__ int ticket_if(int32_t *counter, uint32_t pred) {
-  int v;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\tmov.u32 %0, 0;\n\t"
-      "@p atom.global.add.u32 %0, [%1], 1;\n\t}"
-      : "=r"(v)
-      : "l"(counter), "r"(pred)
-      : "memory");
-  return v;
-}
-
 // 32-bit shared-memory store by the lanes whose pred is set, as predicated PTX.
 __device__ __forceinline__ void st_shared_if(uint32_t addr, uint32_t v, uint32_t pred) {
   asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t@p st.shared.b32 [%0], %1;\n\t}" ::"r"(addr), "r"(v),
                "r"(pred)
-               : "memory");
-}
-
-__device__ __forceinline__ void red_min_if(unsigned long long *addr, unsigned long long v, uint32_t pred) {
-  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t@p red.global.min.u64 [%0], %1;\n\t}" ::"l"(addr),
-               "l"(v), "r"(pred)
                : "memory");
 }
 
@@ -428,23 +410,6 @@ __device__ __forceinline__ void sweep_row_refdel(V (&D)[S], const V (&R)[S], V q
   }
 }
 
-// Warp-wide lexicographic min of (value, column).
-__device__ __forceinline__ void warp_argmin(float &v, int64_t &j) {
-#pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) {
-    const float ov = __shfl_xor_sync(FULL_MASK, v, m);
-    const int64_t oj = __shfl_xor_sync(FULL_MASK, j, m);
-    if (ov < v || (ov == v && (uint64_t)oj < (uint64_t)j)) {
-      v = ov;
-      j = oj;
-    }
-  }
-}
-
-__device__ __forceinline__ unsigned long long make_key(float v, int64_t j) {
-  return ((unsigned long long)float_to_ordered(v) << 32) | (unsigned long long)(uint32_t)j;
-}
-
 // ---------------------------------------------------------------- the persistent kernel
 
 // One REF_DEL row for the policy.
@@ -472,8 +437,10 @@ __device__ __forceinline__ void row(typename Pol<PREC>::V (&D)[S],
 template <int S, int PREC, bool RD, bool ST16 = false>
 constexpr int sdtw_reg_cap() { return S + S * Pol<PREC>::RB / 4 + (RD ? 70 : 40) <= 128 ? 128 : 168; }
 
-// RD: the REF_DEL recurrence (FP32 cells).  A horizontal run can cross any
-// column chunk, so the host gives REF_DEL tasks one chunk (no halo).
+// RD: the REF_DEL recurrence as a row scan, launched for FP16 pairs (FP32
+// cells run the anti-diagonal kernel of refdel.cu, which needs no scan).  A
+// horizontal run can cross any column chunk, so the host gives REF_DEL tasks
+// one chunk (no halo).
 // ST16: FP16 cells whose serving row state is FP16 (p.state_fp16); a separate
 // instance, so the other instances carry none of its registers.
 // NH: halo strips kNarrowHaloCells wide (FP16 pairs, p.narrow_halo).
@@ -1193,8 +1160,6 @@ bool sdtw_instance_exists(int precision, int S, bool ref_del) {
 
 #define DTWX_DISPATCH(PREC, S, CALL) \
   if (precision == PREC && cells_per_thread == S) return CALL<S, PREC>
-#define DTWX_DISPATCH_RD(S, CALL) \
-  if (precision == 1 && cells_per_thread == S) return CALL<S, 1, true>
 #define DTWX_DISPATCH_RD16(S, CALL) \
   if (precision == 0 && cells_per_thread == S) return CALL<S, 0, true>
 #define DTWX_DISPATCH_ST16(S, CALL) \
@@ -1205,8 +1170,8 @@ bool sdtw_instance_exists(int precision, int S, bool ref_del) {
 cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, int grid,
                         const SdtwParams &p, const CUtensorMap *tmap, cudaStream_t s) {
   if (p.ref_del) {
-    DTWX_DISPATCH_RD(16, launch_inst)(warps_per_cta, grid, p, tmap, s);
-    DTWX_DISPATCH_RD(32, launch_inst)(warps_per_cta, grid, p, tmap, s);
+    // FP32 cells: the anti-diagonal kernel of refdel.cu
+    if (precision == 1) return launch_refdel_fp32(cells_per_thread, warps_per_cta, grid, p, s);
     DTWX_DISPATCH_RD16(32, launch_inst)(warps_per_cta, grid, p, tmap, s);
     return cudaErrorInvalidValue;
   }
@@ -1238,8 +1203,7 @@ cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, 
 
 int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta, bool ref_del) {
   if (ref_del) {
-    DTWX_DISPATCH_RD(16, occ_inst)(warps_per_cta);
-    DTWX_DISPATCH_RD(32, occ_inst)(warps_per_cta);
+    if (precision == 1) return refdel_fp32_ctas_per_sm(cells_per_thread, warps_per_cta);
     DTWX_DISPATCH_RD16(32, occ_inst)(warps_per_cta);
     return 0;
   }
