@@ -453,9 +453,10 @@ def run_ours(args, rank, world, local):
     mhz = clock_rec.get("sm_mhz") or 2070.0
     per_sm_cycle = {d.FP16: 64.0, d.FP32: 128.0 / 3.0, d.MIXED: 128.0 / 2.5}[precision]
     if ref_del:
-        # REF_DEL: FP32 cells take 6 + 3 issue slots per cell in the two row passes;
-        # FP16 pairs take 6 FMA-pipe instructions (2 cycles each) per pair
-        per_sm_cycle = 128.0 / 9.0 if precision == d.FP32 else 64.0 / 3.0
+        # REF_DEL: FP32 cells (anti-diagonal sweep) take 4 issue slots per cell
+        # (sub, two mins, FMA); FP16 pairs (row scan) take 6 FMA-pipe
+        # instructions (2 cycles each) per pair
+        per_sm_cycle = 128.0 / 4.0 if precision == d.FP32 else 64.0 / 3.0
     theoretical = sms * per_sm_cycle * mhz * 1e6 / 1e9
     traffic = traffic_from_profile(args.precision, args.workload) if not ref_del else None
     # the roofline peak: the measured probe of the cell's instruction mix where
