@@ -453,10 +453,10 @@ def run_ours(args, rank, world, local):
     mhz = clock_rec.get("sm_mhz") or 2070.0
     per_sm_cycle = {d.FP16: 64.0, d.FP32: 128.0 / 3.0, d.MIXED: 128.0 / 2.5}[precision]
     if ref_del:
-        # REF_DEL: FP32 cells (anti-diagonal sweep) take 4 issue slots per cell
-        # (sub, two mins, FMA); FP16 pairs (row scan) take 6 FMA-pipe
-        # instructions (2 cycles each) per pair
-        per_sm_cycle = 128.0 / 4.0 if precision == d.FP32 else 64.0 / 3.0
+        # REF_DEL (anti-diagonal sweeps): a FP32 cell takes 4 issue slots (sub,
+        # two mins, FMA); a FP16 pair takes the same 4 (HSUB2, two HMNMX2,
+        # HFMA2), its HSUB2 and HFMA2 holding the FMA pipe 2 cycles each
+        per_sm_cycle = 128.0 / 4.0 if precision == d.FP32 else 64.0
     theoretical = sms * per_sm_cycle * mhz * 1e6 / 1e9
     traffic = traffic_from_profile(args.precision, args.workload) if not ref_del else None
     # the roofline peak: the measured probe of the cell's instruction mix where

@@ -300,7 +300,7 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
                   float *state, bool finalize, int &launches) {
   Shape sh = pick_shape(h, precision, n_tasks, mean_rows);
   h->last_shape[precision] = sh;
-  const int pb = sdtw_pair_bytes(precision);
+  const int pb = sdtw_pair_bytes(precision, h->cfg.recurrence == DTWX_REF_DEL);
   int rows_cap = ((max_rows + 1023) / 1024) * 1024;
   if (rows_cap < 1024) rows_cap = 1024;
   const int64_t per_warp = seam_bytes_per_warp(pb, rows_cap);
@@ -570,7 +570,7 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
                                mean_rows, n_reads, reinterpret_cast<const int32_t *>(dm + L.nsamp), d_out,
                                nullptr, false, launches))
       return rc;
-    const int pb = sdtw_pair_bytes(precision);
+    const int pb = sdtw_pair_bytes(precision, h->cfg.recurrence == DTWX_REF_DEL);
     int rows_cap = ((w.max_len + 1023) / 1024) * 1024;
     if (rows_cap < 1024) rows_cap = 1024;
     const int64_t per_warp = seam_bytes_per_warp(pb, rows_cap);

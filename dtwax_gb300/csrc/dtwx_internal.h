@@ -118,8 +118,8 @@ __host__ __device__ inline float ordered_to_float(uint32_t o) {
 // (defined in the .cu files; all return cudaError_t of the launch)
 
 // sDTW over all (task, chunk) items.  precision: 0 FP16, 1 FP32, 2 MIXED;
-// p.ref_del selects the REF_DEL kernels (FP16 pairs: the row scan of sdtw.cu;
-// FP32: the anti-diagonal sweep of refdel.cu).  cells_per_thread must be one
+// p.ref_del selects the REF_DEL kernels (the anti-diagonal sweeps of
+// refdel.cu for FP32 cells and FP16 pairs).  cells_per_thread must be one
 // of the compiled instances.
 cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, int grid,
                         const SdtwParams &p, const CUtensorMap *tmap, cudaStream_t s);
@@ -128,11 +128,15 @@ size_t sdtw_smem_bytes(int precision, int cells_per_thread, int warps_per_cta);
 // Resident CTAs per SM for the given shape (occupancy API), 0 on error.
 int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta, bool ref_del = false);
 bool sdtw_instance_exists(int precision, int cells_per_thread, bool ref_del = false);
-// The FP32 REF_DEL kernel (refdel.cu): 16 or 32 cells per lane, one chunk per task.
+// The REF_DEL kernels of refdel.cu, one chunk per task: FP32 cells (16 or 32
+// cells per lane) and FP16 pairs (32).
 cudaError_t launch_refdel_fp32(int cells_per_thread, int warps_per_cta, int grid, const SdtwParams &p,
                                cudaStream_t s);
 int refdel_fp32_ctas_per_sm(int cells_per_thread, int warps_per_cta);
-int sdtw_pair_bytes(int precision);  // bytes per DP cell (seam scratch)
+cudaError_t launch_refdel_pairs(int cells_per_thread, int warps_per_cta, int grid, const SdtwParams &p,
+                                cudaStream_t s);
+int refdel_pairs_ctas_per_sm(int cells_per_thread, int warps_per_cta);
+int sdtw_pair_bytes(int precision, bool ref_del = false);  // bytes per seam entry (per row)
 int sdtw_ref_bytes(int precision);   // reference bytes per column of a strip
 
 // Reference builder: genome bytes -> z-scored levels as FP16 (fwd, rev) pairs,

@@ -1142,7 +1142,10 @@ static int occ_inst(int warps) {
   return n;
 }
 
-int sdtw_pair_bytes(int precision) { (void)precision; return 4; }
+int sdtw_pair_bytes(int precision, bool ref_del) {
+  // the FP16-pair REF_DEL kernel passes its seam column as absolute FP32 pairs
+  return precision == 0 && ref_del ? 8 : 4;
+}
 
 int sdtw_ref_bytes(int precision) { return precision == 2 ? 2 : 4; }
 
@@ -1160,8 +1163,6 @@ bool sdtw_instance_exists(int precision, int S, bool ref_del) {
 
 #define DTWX_DISPATCH(PREC, S, CALL) \
   if (precision == PREC && cells_per_thread == S) return CALL<S, PREC>
-#define DTWX_DISPATCH_RD16(S, CALL) \
-  if (precision == 0 && cells_per_thread == S) return CALL<S, 0, true>
 #define DTWX_DISPATCH_ST16(S, CALL) \
   if (precision == 0 && cells_per_thread == S) return CALL<S, 0, false, true>
 #define DTWX_DISPATCH_NH(S, ST16, CALL) \
@@ -1170,9 +1171,9 @@ bool sdtw_instance_exists(int precision, int S, bool ref_del) {
 cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, int grid,
                         const SdtwParams &p, const CUtensorMap *tmap, cudaStream_t s) {
   if (p.ref_del) {
-    // FP32 cells: the anti-diagonal kernel of refdel.cu
+    // the anti-diagonal kernels of refdel.cu
     if (precision == 1) return launch_refdel_fp32(cells_per_thread, warps_per_cta, grid, p, s);
-    DTWX_DISPATCH_RD16(32, launch_inst)(warps_per_cta, grid, p, tmap, s);
+    if (precision == 0) return launch_refdel_pairs(cells_per_thread, warps_per_cta, grid, p, s);
     return cudaErrorInvalidValue;
   }
   if (p.narrow_halo) {
@@ -1204,7 +1205,7 @@ cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, 
 int sdtw_ctas_per_sm(int precision, int cells_per_thread, int warps_per_cta, bool ref_del) {
   if (ref_del) {
     if (precision == 1) return refdel_fp32_ctas_per_sm(cells_per_thread, warps_per_cta);
-    DTWX_DISPATCH_RD16(32, occ_inst)(warps_per_cta);
+    if (precision == 0) return refdel_pairs_ctas_per_sm(cells_per_thread, warps_per_cta);
     return 0;
   }
   DTWX_DISPATCH(0, 32, occ_inst)(warps_per_cta);
