@@ -320,105 +320,7 @@ __device__ __forceinline__ void sweep_row_mixed(float (&D)[S], const __half2 (&R
   }
 }
 
-// The REF_DEL row: the cell to the left in the same row is a third
-// predecessor, D[j] = min(v[j], c[j] + D[j-1]) with c = d^2 and
-// v = c + min(up, diag).  That is a scan along the row in the (min, +)
-// semiring, done in three passes:
-//  1. each lane runs its S columns with +inf entering on the left, keeping the
-//     local values P[j] in D and the lane's map x -> min(P[S-1], x + sum c);
-//     the S columns are two halves run as two independent chains (twice the
-//     instruction-level parallelism), whose maps are then composed;
-//  2. the 32 lane maps are composed by a warp scan, (a1, b1) then (a2, b2)
-//     being (a1 + a2, min(b2, b1 + a2)), which gives each lane its left input;
-//  3. D[j] = min(P[j], X + c[0] + ... + c[j]), again as two chains.
-// seam_diag / seam_left are the left strip's last column on the previous and
-// on this row (lane 0 only).  RdOps is the arithmetic of the cell type.
-template <typename V>
-struct RdOps;
-template <>
-struct RdOps<float> {
-  __device__ __forceinline__ static float sub(float a, float b) { return a - b; }
-  __device__ __forceinline__ static float add(float a, float b) { return a + b; }
-  __device__ __forceinline__ static float fma(float a, float b, float c) { return fmaf(a, b, c); }
-  __device__ __forceinline__ static float vmin(float a, float b) { return fminf(a, b); }
-  __device__ __forceinline__ static float inf() { return __int_as_float(0x7f800000); }
-  __device__ __forceinline__ static float zero() { return 0.f; }
-  __device__ __forceinline__ static uint32_t bits(float v) { return __float_as_uint(v); }
-};
-template <>
-struct RdOps<__half2> {
-  // FP16 pairs in the strip's running-minimum frame; cost sums that overflow
-  // half become +inf, which only drops left-boundary paths far above every
-  // cell of the row
-  __device__ __forceinline__ static __half2 sub(__half2 a, __half2 b) { return __hsub2(a, b); }
-  __device__ __forceinline__ static __half2 add(__half2 a, __half2 b) { return __hadd2(a, b); }
-  __device__ __forceinline__ static __half2 fma(__half2 a, __half2 b, __half2 c) { return __hfma2(a, b, c); }
-  __device__ __forceinline__ static __half2 vmin(__half2 a, __half2 b) { return __hmin2(a, b); }
-  __device__ __forceinline__ static __half2 inf() { return Pol<0>::inf(); }
-  __device__ __forceinline__ static __half2 zero() { return Pol<0>::zero(); }
-  __device__ __forceinline__ static uint32_t bits(__half2 v) { return cell_bits<0>(v); }
-};
-
-template <int S, typename V>
-__device__ __forceinline__ void sweep_row_refdel(V (&D)[S], const V (&R)[S], V q, V seam_diag, V seam_left,
-                                                 uint32_t m0, int lane) {
-  using O = RdOps<V>;
-  constexpr int H = S / 2;
-  const V up = __shfl_up_sync(FULL_MASK, D[S - 1], 1);
-  V dp0 = bits_as<V>((O::bits(up) & ~m0) | (O::bits(seam_diag) & m0));
-  V dp1 = D[H - 1];  // the previous row's value left of the second half
-  V p0 = O::inf(), p1 = O::inf(), a0 = O::zero(), a1 = O::zero();
-#pragma unroll
-  for (int k = 0; k < H; ++k) {
-    const V t0 = D[k], t1 = D[H + k];
-    const V d0 = O::sub(R[k], q), d1 = O::sub(R[H + k], q);
-    const V v0 = O::fma(d0, d0, O::vmin(t0, dp0));
-    const V v1 = O::fma(d1, d1, O::vmin(t1, dp1));
-    dp0 = t0;
-    dp1 = t1;
-    p0 = O::vmin(v0, O::fma(d0, d0, p0));
-    p1 = O::vmin(v1, O::fma(d1, d1, p1));
-    a0 = O::fma(d0, d0, a0);
-    a1 = O::fma(d1, d1, a1);
-    D[k] = p0;
-    D[H + k] = p1;
-  }
-  // the lane's map: the first half's map, then the second half's
-  V a = O::add(a0, a1);
-  V b = O::vmin(p1, O::add(p0, a1));
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const V ua = __shfl_up_sync(FULL_MASK, a, off);
-    const V ub = __shfl_up_sync(FULL_MASK, b, off);
-    const bool act = lane >= off;
-    b = act ? O::vmin(b, O::add(ub, a)) : b;
-    a = act ? O::add(ua, a) : a;
-  }
-  // exclusive prefix: the composed map of lanes 0..l-1 applied to seam_left
-  const V ea = __shfl_up_sync(FULL_MASK, a, 1);
-  const V eb = __shfl_up_sync(FULL_MASK, b, 1);
-  const V xin = O::vmin(eb, O::add(seam_left, ea));
-  V x0 = bits_as<V>((O::bits(xin) & ~m0) | (O::bits(seam_left) & m0));
-  V x1 = O::vmin(p0, O::add(x0, a0));  // the true value left of the second half
-#pragma unroll
-  for (int k = 0; k < H; ++k) {
-    const V d0 = O::sub(R[k], q), d1 = O::sub(R[H + k], q);
-    x0 = O::fma(d0, d0, x0);
-    x1 = O::fma(d1, d1, x1);
-    D[k] = O::vmin(D[k], x0);
-    D[H + k] = O::vmin(D[H + k], x1);
-  }
-}
-
 // ---------------------------------------------------------------- the persistent kernel
-
-// One REF_DEL row for the policy.
-template <int S, int PREC>
-__device__ __forceinline__ void row_refdel(typename Pol<PREC>::V (&D)[S], const typename Pol<PREC>::RV (&R)[S],
-                                           typename Pol<PREC>::QW qq, typename Pol<PREC>::V seam_diag,
-                                           typename Pol<PREC>::V seam_left, uint32_t m0, int lane) {
-  sweep_row_refdel<S, typename Pol<PREC>::V>(D, R, qq, seam_diag, seam_left, m0, lane);
-}
 
 // One DP row for the policy: FP16 pairs and FP32 share sweep_row, MIXED has its own.
 template <int S, int PREC>
@@ -432,20 +334,18 @@ __device__ __forceinline__ void row(typename Pol<PREC>::V (&D)[S],
 }
 
 // Register cap per instance: the S cells and S reference elements of a lane
-// plus about 40 registers of bookkeeping (70 for the REF_DEL scan), rounded to
-// 128 or 168 (16 or 12 warps/SM).
-template <int S, int PREC, bool RD, bool ST16 = false>
-constexpr int sdtw_reg_cap() { return S + S * Pol<PREC>::RB / 4 + (RD ? 70 : 40) <= 128 ? 128 : 168; }
+// plus about 40 registers of bookkeeping, rounded to 128 or 168 (16 or 12
+// warps/SM).
+template <int S, int PREC>
+constexpr int sdtw_reg_cap() { return S + S * Pol<PREC>::RB / 4 + 40 <= 128 ? 128 : 168; }
 
-// RD: the REF_DEL recurrence as a row scan, launched for FP16 pairs (FP32
-// cells run the anti-diagonal kernel of refdel.cu, which needs no scan).  A
-// horizontal run can cross any column chunk, so the host gives REF_DEL tasks
-// one chunk (no halo).
+// The NO_REF_DEL sweep.  (The REF_DEL recurrence runs the anti-diagonal
+// kernels of refdel.cu.)
 // ST16: FP16 cells whose serving row state is FP16 (p.state_fp16); a separate
 // instance, so the other instances carry none of its registers.
 // NH: halo strips kNarrowHaloCells wide (FP16 pairs, p.narrow_halo).
-template <int S, int PREC, bool RD, bool ST16, bool NH>
-__global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
+template <int S, int PREC, bool ST16, bool NH>
+__global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(
     const __grid_constant__ CUtensorMap tmap, const SdtwParams p) {
   using P = Pol<PREC>;
   using V = typename P::V;
@@ -460,11 +360,9 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
   constexpr int SH = NH ? kNarrowHaloCells : S;  // cells per lane in halo strips
   constexpr int WH = kWarp * SH;
   static_assert(S % SH == 0 && SH % 8 == 0, "halo strips must tile the chunk start");
-  static_assert(!NH || (PREC == 0 && !RD), "narrow halo strips are built for FP16 pairs (REF_DEL has no halo)");
+  static_assert(!NH || PREC == 0, "narrow halo strips are built for FP16 pairs");
   static_assert(STRIP_BYTES % 1024 == 0, "strip tile must keep 1024-byte alignment");
   static_assert(S % 8 == 0, "row state and reference move in 16-byte groups");
-  static_assert(!RD || PREC <= 1, "the REF_DEL row is built for FP16 pairs and FP32 cells");
-  static_assert(!(RD && ST16), "REF_DEL with the FP16 row state is not built");
   static_assert(!ST16 || PREC == 0, "the FP16 row state is built for FP16 cells");
 
   extern __shared__ unsigned char smem_raw[];
@@ -702,36 +600,21 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
       // frame (delta changes only at a rescale, which ends a window)
       const V vinf = P::inf();
       typename P::QW qwin = P::qw(lane < n ? q[lane] : 0.f);
-      // REF_DEL also reads the seam value of the last row itself (one entry further)
-      constexpr int kExtra = RD ? 1 : 0;
-      V swin = (!first && lane < rows + kExtra) ? seam_in[lane] : vinf;
+      V swin = (!first && lane < rows) ? seam_in[lane] : vinf;
       if constexpr (PREC == 0) swin = __hadd2(swin, delta);
       V *so = seam_out + 1;  // seam value of row i goes to seam_out[i + 1]
       for (int i0 = 0; i0 < rows; i0 += kWarp) {
         const int r = i0 + kWarp + lane;
         const float qn = r < n ? q[r] : 0.f;
-        const V sn = (!first && r < rows + kExtra) ? seam_in[r] : vinf;
+        const V sn = (!first && r < rows) ? seam_in[r] : vinf;
         // the seam column leaving this strip is gathered in a register window
         // (lane l keeps row i0+l) and stored once per 32 rows, coalesced: no
         // lane-conditional store inside the row loop
         V sout = vinf;
-        // REF_DEL: lane l of lwin holds the left strip's value on row i0+l itself
-        V lwin = vinf;
-        if constexpr (RD) {
-          V last = P::shfl(sn, 0);  // the left strip's value on row i0+31, stored after its rescale
-          if constexpr (PREC == 0) {
-            // that value is in the left strip's next frame: re-base with the next epoch's offset
-            last = __hadd2(last, __float22half2_rn(make_float2(off_next.x - O.x, off_next.y - O.y)));
-          }
-          lwin = P::sel(lane == kWarp - 1, last, __shfl_down_sync(FULL_MASK, swin, 1));
-        }
         if (rows - i0 >= kWarp) {
   #pragma unroll 4
           for (int il = 0; il < kWarp; ++il) {
-            if constexpr (RD)
-              row_refdel<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
-            else
-              row<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+            row<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
             if constexpr (SMEM_SEAM)
               st_shared_if(sob + 4u * (uint32_t)il, cell_bits<PREC>(D[SH - 1]), is31);
             else
@@ -766,10 +649,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
         } else {
           const int cnt = rows - i0;
           for (int il = 0; il < cnt; ++il) {
-            if constexpr (RD)
-              row_refdel<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
-            else
-              row<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+            row<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
             if constexpr (SMEM_SEAM)
               st_shared_if(sob + 4u * (uint32_t)il, cell_bits<PREC>(D[SH - 1]), is31);
             else
@@ -954,36 +834,21 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
       // frame (delta changes only at a rescale, which ends a window)
       const V vinf = P::inf();
       typename P::QW qwin = P::qw(lane < n ? q[lane] : 0.f);
-      // REF_DEL also reads the seam value of the last row itself (one entry further)
-      constexpr int kExtra = RD ? 1 : 0;
-      V swin = (!first && lane < rows + kExtra) ? seam_in[lane] : vinf;
+      V swin = (!first && lane < rows) ? seam_in[lane] : vinf;
       if constexpr (PREC == 0) swin = __hadd2(swin, delta);
       V *so = seam_out + 1;  // seam value of row i goes to seam_out[i + 1]
       for (int i0 = 0; i0 < rows; i0 += kWarp) {
         const int r = i0 + kWarp + lane;
         const float qn = r < n ? q[r] : 0.f;
-        const V sn = (!first && r < rows + kExtra) ? seam_in[r] : vinf;
+        const V sn = (!first && r < rows) ? seam_in[r] : vinf;
         // the seam column leaving this strip is gathered in a register window
         // (lane l keeps row i0+l) and stored once per 32 rows, coalesced: no
         // lane-conditional store inside the row loop
         V sout = vinf;
-        // REF_DEL: lane l of lwin holds the left strip's value on row i0+l itself
-        V lwin = vinf;
-        if constexpr (RD) {
-          V last = P::shfl(sn, 0);  // the left strip's value on row i0+31, stored after its rescale
-          if constexpr (PREC == 0) {
-            // that value is in the left strip's next frame: re-base with the next epoch's offset
-            last = __hadd2(last, __float22half2_rn(make_float2(off_next.x - O.x, off_next.y - O.y)));
-          }
-          lwin = P::sel(lane == kWarp - 1, last, __shfl_down_sync(FULL_MASK, swin, 1));
-        }
         if (rows - i0 >= kWarp) {
 #pragma unroll 4
           for (int il = 0; il < kWarp; ++il) {
-            if constexpr (RD)
-              row_refdel<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
-            else
-              row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+            row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
             if constexpr (SMEM_SEAM)
               st_shared_if(sob + 4u * (uint32_t)il, cell_bits<PREC>(D[S - 1]), is31);
             else
@@ -1018,10 +883,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
         } else {
           const int cnt = rows - i0;
           for (int il = 0; il < cnt; ++il) {
-            if constexpr (RD)
-              row_refdel<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), P::shfl(lwin, il), m0, lane);
-            else
-              row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
+            row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
             if constexpr (SMEM_SEAM)
               st_shared_if(sob + 4u * (uint32_t)il, cell_bits<PREC>(D[S - 1]), is31);
             else
@@ -1115,11 +977,11 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC, RD, ST16>())) sdtw_kernel(
 
 // ---------------------------------------------------------------- instances / launch
 
-template <int S, int PREC, bool RD = false, bool ST16 = false, bool NH = false>
+template <int S, int PREC, bool ST16 = false, bool NH = false>
 static cudaError_t launch_inst(int warps, int grid, const SdtwParams &p, const CUtensorMap *tmap,
                                cudaStream_t s) {
   const size_t smem = sdtw_smem_bytes(PREC, S, warps);
-  auto fn = sdtw_kernel<S, PREC, RD, ST16, NH>;
+  auto fn = sdtw_kernel<S, PREC, ST16, NH>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   CUtensorMap dummy;
@@ -1131,11 +993,11 @@ static cudaError_t launch_inst(int warps, int grid, const SdtwParams &p, const C
   return cudaGetLastError();
 }
 
-template <int S, int PREC, bool RD = false, bool ST16 = false, bool NH = false>
+template <int S, int PREC, bool ST16 = false, bool NH = false>
 static int occ_inst(int warps) {
   int n = 0;
   const size_t smem = sdtw_smem_bytes(PREC, S, warps);
-  auto fn = sdtw_kernel<S, PREC, RD, ST16, NH>;
+  auto fn = sdtw_kernel<S, PREC, ST16, NH>;
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, warps * kWarp, smem) != cudaSuccess) return 0;
@@ -1164,9 +1026,9 @@ bool sdtw_instance_exists(int precision, int S, bool ref_del) {
 #define DTWX_DISPATCH(PREC, S, CALL) \
   if (precision == PREC && cells_per_thread == S) return CALL<S, PREC>
 #define DTWX_DISPATCH_ST16(S, CALL) \
-  if (precision == 0 && cells_per_thread == S) return CALL<S, 0, false, true>
+  if (precision == 0 && cells_per_thread == S) return CALL<S, 0, true>
 #define DTWX_DISPATCH_NH(S, ST16, CALL) \
-  if (precision == 0 && cells_per_thread == S) return CALL<S, 0, false, ST16, true>
+  if (precision == 0 && cells_per_thread == S) return CALL<S, 0, ST16, true>
 
 cudaError_t launch_sdtw(int precision, int cells_per_thread, int warps_per_cta, int grid,
                         const SdtwParams &p, const CUtensorMap *tmap, cudaStream_t s) {
