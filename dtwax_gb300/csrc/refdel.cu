@@ -1,5 +1,6 @@
-// The REF_DEL recurrence on FP32 cells (src/include/DTW.cu:23-29, the build
-// without -DNO_REF_DEL; scripts/sdtw.py keeps no such variant):
+// The REF_DEL recurrence on FP32 cells and on FP16 pairs (src/include/DTW.cu:
+// 23-29, the build without -DNO_REF_DEL; scripts/sdtw.py keeps no such
+// variant):
 //
 //   D[i][j] = (r_j - q_i)^2 + min(D[i-1][j], D[i-1][j-1], D[i][j-1])
 //
@@ -23,8 +24,10 @@
 // rows and keep their cells, so after the last step every lane holds row
 // n - 1.
 //
-// A horizontal run can cross any column, so a task is one work item per
-// strand that sweeps every strip (the host launches it with one chunk).
+// A horizontal run can cross any column, so a task is one work item (per
+// strand for FP32 cells) that sweeps every strip (the host launches it with
+// one chunk).  The FP16-pair kernel further down adds per-lane
+// running-minimum frames.
 #include "dtwx_internal.h"
 #include "warp_ops.cuh"
 
