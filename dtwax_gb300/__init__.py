@@ -30,6 +30,7 @@ FP16, FP32, MIXED = 0, 1, 2  # MIXED: FP16 differences, FP32 path cost
 NO_REF_DEL, REF_DEL = 0, 1     # recurrence: without / with the left predecessor
 STATE_FP32, STATE_FP16 = 0, 1  # serving row state
 STRANDS_PAIRED, STRANDS_CONCAT = 0, 1
+CALL_DEVICE_ERROR = -2  # dtwx_result.call of reads whose call hit a device-side error
 ABI_VERSION = 2
 
 
@@ -102,6 +103,8 @@ _SIGNATURES = {
     "dtwx_classify_batch_i16": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P, _P, _P, _P]),
     "dtwx_distances": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P, _P]),
     "dtwx_classify_device": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P, _P]),
+    "dtwx_sync": (ctypes.c_int, [_P]),
+    "dtwx_debug_stall_next": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_uint32]),
     "dtwx_classify_plain_fp32": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P]),
     "dtwx_distances_static": (ctypes.c_int, [_P, ctypes.c_int64, _P, _I64P, ctypes.c_int32, ctypes.c_float, _P, _P]),
     "dtwx_last_launch_count": (ctypes.c_int32, [_P]),
@@ -290,6 +293,17 @@ class Classifier:
         _check(self._lib.dtwx_classify_device(self._h, ctypes.c_void_p(d_raw), offsets.ctypes.data_as(_I64P),
                                               offsets.size - 1, ctypes.c_void_p(d_out), ctypes.c_void_p(stream)),
                self._h)
+
+    def sync(self):
+        """Wait for the last device-pointer call (distances / classify_device)
+        and raise DtwxError if its kernels reported a device-side error."""
+        _check(self._lib.dtwx_sync(self._h), self._h)
+
+    def debug_stall_next(self, item: int, spin_limit: int = 0):
+        """Test hook: the next sweep withholds the first reference-strip copy of
+        work item `item`, so that item's bounded wait runs out (after
+        spin_limit polls, 0 = the library's limit)."""
+        _check(self._lib.dtwx_debug_stall_next(self._h, int(item), int(spin_limit)), self._h)
 
     @property
     def last_launch_count(self) -> int:

@@ -109,6 +109,12 @@ struct dtwx_handle {
   std::string err;
   int32_t last_launches = 0;
   Shape last_shape[3];
+  // a device-pointer call (dtwx_distances / dtwx_classify_device) was enqueued
+  // since the last dtwx_sync; ctx[0].done marks its end on the caller's stream
+  bool device_call_pending = false;
+  // one-shot test hook of dtwx_debug_stall_next for the next sweep launch
+  int32_t stall_item = 0;
+  uint32_t stall_spin = 0;
   // serving
   bool serving = false;
   int32_t chunks_per_decision = 3;
@@ -315,7 +321,7 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
   }
   int32_t *counter = c.flags.as<int32_t>();
   int32_t *err = counter + 4;
-  CK(h, launch_reset(c.keys.as<unsigned long long>(), 2 * n_slots, counter, st));
+  CK(h, launch_reset(c.keys.as<unsigned long long>(), 2 * n_slots, counter, err, st));
   ++launches;
   if (n_tasks > 0) {
     SdtwParams p{};
@@ -343,6 +349,10 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
     p.ref_del = h->cfg.recurrence == DTWX_REF_DEL ? 1 : 0;
     p.state_fp16 = state_fp16(h) ? 1 : 0;
     p.narrow_halo = sh.nh ? 1 : 0;
+    p.stall_item = h->stall_item;
+    p.spin_limit = h->stall_spin;
+    h->stall_item = 0;
+    h->stall_spin = 0;
     const int ii = inst_index(precision, sh.S);
     p.use_tma = h->tmap_ok[precision][ii] ? 1 : 0;
     // inside a stream capture the timing events become event-record nodes
@@ -356,7 +366,7 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
   }
   if (finalize) {
     CK(h, launch_finalize(c.keys.as<unsigned long long>(), d_nsamp, n_slots,
-                          h->cfg.strand_mode == DTWX_STRANDS_CONCAT, h->m, h->cfg.threshold, d_out, st));
+                          h->cfg.strand_mode == DTWX_STRANDS_CONCAT, h->m, h->cfg.threshold, err, d_out, st));
     ++launches;
   }
   return DTWX_OK;
@@ -615,8 +625,8 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
       ++launches;
     }
     CK(h, launch_finalize(c.keys.as<unsigned long long>(), reinterpret_cast<const int32_t *>(dm + L.nsamp),
-                          n_reads, h->cfg.strand_mode == DTWX_STRANDS_CONCAT, h->m, h->cfg.threshold, d_out,
-                          st));
+                          n_reads, h->cfg.strand_mode == DTWX_STRANDS_CONCAT, h->m, h->cfg.threshold,
+                          c.flags.as<int32_t>() + 4, d_out, st));
     ++launches;
   }
   h->last_launches = launches;
@@ -642,6 +652,10 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
     CK(h, cudaStreamSynchronize(st));
     c.meta_pending = false;
     if (int rc = check_device_flags(h, c)) return rc;
+  } else {
+    // device results: the error word is read by dtwx_sync (and marked in the results)
+    CK(h, cudaEventRecord(c.done, st));
+    h->device_call_pending = true;
   }
   return DTWX_OK;
 }
@@ -956,7 +970,28 @@ int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets,
                          n_tasks ? sum / n_tasks : 0.0, n_reads, reinterpret_cast<const int32_t *>(dm + L.nsamp),
                          d_out, nullptr, true, launches);
   h->last_launches = launches;
-  return rc;
+  if (rc) return rc;
+  CK(h, cudaEventRecord(c.done, st));
+  h->device_call_pending = true;
+  return DTWX_OK;
+}
+
+int dtwx_sync(dtwx_handle *h) {
+  if (!h) return DTWX_E_ARG;
+  CK(h, cudaSetDevice(h->device));
+  BatchCtx &c = h->ctx[0];
+  if (!h->device_call_pending) return DTWX_OK;
+  CK(h, cudaEventSynchronize(c.done));
+  h->device_call_pending = false;
+  return check_device_flags(h, c);
+}
+
+int dtwx_debug_stall_next(dtwx_handle *h, int32_t item, uint32_t spin_limit) {
+  if (!h) return DTWX_E_ARG;
+  if (item < 0) return fail(h, DTWX_E_ARG, "item must be >= 0");
+  h->stall_item = item + 1;
+  h->stall_spin = spin_limit;
+  return DTWX_OK;
 }
 
 int dtwx_autotune(dtwx_handle *h, int32_t n_reads_req, int32_t read_len, float *best_ms) {

@@ -25,8 +25,12 @@ constexpr int kRescaleRows = 32;
 // otherwise change.
 constexpr int kNarrowHaloCells = 16;
 constexpr int kNarrowHaloMaxStrips = 32;
-// Bounded device-side waits: iterations before a wait gives up and flags an error.
-constexpr uint32_t kSpinLimit = 1u << 26;
+// Bounded device-side waits: polls of mbarrier.try_wait before a wait gives up
+// and flags an error.  A poll that finds the phase incomplete suspends the
+// warp for a few microseconds (measured on GB300: 4,096 polls in about 15 ms),
+// so 2^18 polls bound a wait at about one second; a strip copy lands in
+// microseconds.  The count does not advance while the context is switched out.
+constexpr uint32_t kSpinLimit = 1u << 18;
 
 // Task flags.
 constexpr int32_t kTaskResume = 1;    // start from the saved row state instead of free start
@@ -48,6 +52,9 @@ static_assert(sizeof(Task) == 32, "Task layout");
 // Device error flags (bit mask in *err).
 constexpr int32_t kErrTmaTimeout = 1;
 constexpr int32_t kErrBadTask = 2;
+// dtwx_result.call of every read of a call whose kernels set a device error
+// flag (DTWX_CALL_DEVICE_ERROR of include/dtwx.h).
+constexpr int32_t kCallDeviceError = -2;
 
 struct SdtwParams {
   const float *query;          // z-scored samples, FP32
@@ -76,6 +83,9 @@ struct SdtwParams {
   int32_t state_fp16;          // FP16 cells: row state as half2 cells (m_pad) then one float2
                                // frame offset per 512-column group (m_pad / 512)
   int32_t narrow_halo;         // FP16 pairs: launch the instance with kNarrowHaloCells-wide halo strips
+  uint32_t spin_limit;         // polls before a bounded wait gives up; 0 = kSpinLimit
+  int32_t stall_item;          // test hook: 1 + the queue ticket whose first reference-strip copy
+                               // is not issued, so that its warp's bounded wait runs out; 0 = none
 };
 
 // Per-warp scratch layout, in bytes, for cells of `pair_bytes` bytes.
@@ -83,14 +93,13 @@ struct SdtwParams {
 // cells plus 32 of slack (whole-warp stores past the last row land there),
 // then from a 16-byte aligned position the FP32 offsets of the epochs,
 // (max_rows / kRescaleRows + 2) float2 plus 32 of slack.
-inline __host__ __device__ int64_t seam_offsets_pos(int pair_bytes, int max_rows) {
+constexpr __host__ __device__ int64_t seam_offsets_pos(int pair_bytes, int max_rows) {
   return ((int64_t)(max_rows + 1 + 32) * pair_bytes + 15) & ~(int64_t)15;
 }
-inline __host__ __device__ int64_t seam_bytes_per_warp(int pair_bytes, int max_rows) {
-  const int64_t epochs = (int64_t)(max_rows / kRescaleRows + 2 + 32) * 8;
-  int64_t per = seam_offsets_pos(pair_bytes, max_rows) + epochs;
-  per = (per + 255) & ~(int64_t)255;
-  return 2 * per;  // ping-pong between consecutive strips
+constexpr __host__ __device__ int64_t seam_bytes_per_warp(int pair_bytes, int max_rows) {
+  // ping-pong between consecutive strips
+  return 2 * ((seam_offsets_pos(pair_bytes, max_rows) + (int64_t)(max_rows / kRescaleRows + 2 + 32) * 8 + 255) &
+              ~(int64_t)255);
 }
 
 // Orderable 32-bit image of a float: unsigned order == float order.
@@ -155,13 +164,17 @@ cudaError_t launch_normalize(const void *src, int is_i16, const int64_t *src_off
                              const float *scale_mul, const float *scale_add, int n_reads,
                              float eps, float *dst, cudaStream_t s);
 
-// Keys -> dtwx_result records.
+// Keys -> dtwx_result records.  When the device error word `err` (may be
+// NULL) is non-zero, every record of the call is marked call =
+// DTWX_CALL_DEVICE_ERROR with the error bits in `strand` and NaN scores: the
+// sweep did not finish, so no score of the call can be trusted.
 cudaError_t launch_finalize(const unsigned long long *keys, const int32_t *n_samples,
                             int n_reads, int concat, int64_t m_fwd, float threshold,
-                            void *d_results, cudaStream_t s);
+                            const int32_t *err, void *d_results, cudaStream_t s);
 
-// Reset keys to the empty value and the work counter to zero.
-cudaError_t launch_reset(unsigned long long *keys, int n_keys, int32_t *counter,
+// Reset keys to the empty value, the work counter and the device error word
+// (either may be NULL) to zero.
+cudaError_t launch_reset(unsigned long long *keys, int n_keys, int32_t *counter, int32_t *err,
                          cudaStream_t s);
 
 // Record the message dtwx_last_error(NULL) reports (calls made without a handle).

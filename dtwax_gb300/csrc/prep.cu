@@ -253,15 +253,17 @@ cudaError_t launch_normalize(const void *src, int is_i16, const int64_t *src_off
 
 // ---------------------------------------------------------------- reset / finalize
 
-__global__ void reset_kernel(unsigned long long *keys, int n_keys, int32_t *counter) {
+__global__ void reset_kernel(unsigned long long *keys, int n_keys, int32_t *counter, int32_t *err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n_keys) keys[i] = ~0ull;
   if (i == 0 && counter) *counter = 0;
+  if (i == 0 && err) *err = 0;
 }
 
-cudaError_t launch_reset(unsigned long long *keys, int n_keys, int32_t *counter, cudaStream_t s) {
+cudaError_t launch_reset(unsigned long long *keys, int n_keys, int32_t *counter, int32_t *err,
+                         cudaStream_t s) {
   const int n = n_keys > 1 ? n_keys : 1;
-  reset_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(keys, n_keys, counter);
+  reset_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(keys, n_keys, counter, err);
   return cudaGetLastError();
 }
 
@@ -272,7 +274,7 @@ cudaError_t launch_reset(unsigned long long *keys, int n_keys, int32_t *counter,
 // made: target when score < threshold (calc_classification_threshold.py:52).
 __global__ void finalize_kernel(const unsigned long long *keys, const int32_t *n_samples,
                                 int n_reads, int concat, int64_t m_fwd, float threshold,
-                                ResultRec *out) {
+                                const int32_t *err, ResultRec *out) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_reads) return;
   ResultRec o;
@@ -305,15 +307,23 @@ __global__ void finalize_kernel(const unsigned long long *keys, const int32_t *n
     o.end_pos = -1;
     o.strand = 0;
   }
+  const int32_t e = err ? *err : 0;
+  if (e != 0) {
+    // a bounded wait gave up or a task was refused: the keys are incomplete
+    o.score = o.score_fwd = o.score_rev = __int_as_float(0x7fc00000);
+    o.end_pos = -1;
+    o.strand = e;
+    o.call = kCallDeviceError;
+  }
   out[r] = o;
 }
 
 cudaError_t launch_finalize(const unsigned long long *keys, const int32_t *n_samples, int n_reads,
-                            int concat, int64_t m_fwd, float threshold, void *d_results,
-                            cudaStream_t s) {
+                            int concat, int64_t m_fwd, float threshold, const int32_t *err,
+                            void *d_results, cudaStream_t s) {
   if (n_reads <= 0) return cudaSuccess;
   finalize_kernel<<<(n_reads + kBlock - 1) / kBlock, kBlock, 0, s>>>(
-      keys, n_samples, n_reads, concat, m_fwd, threshold, static_cast<ResultRec *>(d_results));
+      keys, n_samples, n_reads, concat, m_fwd, threshold, err, static_cast<ResultRec *>(d_results));
   return cudaGetLastError();
 }
 

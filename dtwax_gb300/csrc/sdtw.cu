@@ -154,10 +154,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                : "memory");
 }
 
-// Bounded wait on an mbarrier phase; false when the wait gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Bounded wait on an mbarrier phase: at most `limit` polls; false when the
+// wait gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit) {
   const uint32_t addr = smem_u32(bar);
-  for (uint32_t it = 0; it < kSpinLimit; ++it) {
+  for (uint32_t it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -402,6 +403,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(
   const int nstr = !PAIRS ? (p.strands > 0 ? p.strands : 2) : 1;
   const int per_task = p.n_chunks * nstr;
   const int64_t n_items = (int64_t)p.n_tasks * per_task;
+  const uint32_t spin_limit = p.spin_limit ? p.spin_limit : kSpinLimit;
 
   for (;;) {
     const int item = __shfl_sync(FULL_MASK, ticket_if(p.counter, is0), 0);
@@ -444,8 +446,11 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(
     int64_t colx = -1, coly = -1;
 
     if (p.use_tma) {
+      // the test hook p.stall_item withholds this copy (and its arrival) for
+      // one item: the strip's wait below then runs out with no copy in flight
       fence_proxy_async_smem();
-      tma_issue_if(slot0, &tmap, &bars[0], 0, (int)((ref_plane + x0) * RB / 128), STRIP_BYTES, is0);
+      tma_issue_if(slot0, &tmap, &bars[0], 0, (int)((ref_plane + x0) * RB / 128), STRIP_BYTES,
+                   is0 & (item + 1 != p.stall_item ? 1u : 0u));
     }
 
     // One narrow halo strip (SH cells per lane, left of column a); false if a
@@ -554,7 +559,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(
       if (p.use_tma) {
         const int sl = s & 1;
         // every lane waits (acquire of the TMA bytes); the give-up decision is warp-uniform
-        const bool ok = __all_sync(FULL_MASK, mbar_wait(&bars[sl], (phase >> sl) & 1u));
+        const bool ok = __all_sync(FULL_MASK, mbar_wait(&bars[sl], (phase >> sl) & 1u, spin_limit));
         if (!ok) {
           atomicOr(p.err, kErrTmaTimeout);  // every lane: same bit
           return false;
@@ -789,7 +794,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(
       if (p.use_tma) {
         const int sl = s & 1;
         // every lane waits (acquire of the TMA bytes); the give-up decision is warp-uniform
-        const bool ok = __all_sync(FULL_MASK, mbar_wait(&bars[sl], (phase >> sl) & 1u));
+        const bool ok = __all_sync(FULL_MASK, mbar_wait(&bars[sl], (phase >> sl) & 1u, spin_limit));
         if (!ok) {
           atomicOr(p.err, kErrTmaTimeout);  // every lane: same bit
           return;

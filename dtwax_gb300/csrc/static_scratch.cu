@@ -27,10 +27,13 @@ constexpr int kStCtas = 64;         // CTAs: 256 warps share the queue
 constexpr int kStPairBytes = 8;     // float2 (fwd, rev)
 
 constexpr int64_t align256(int64_t x) { return (x + 255) & ~(int64_t)255; }
-// seam layout of one warp, the same arithmetic as seam_bytes_per_warp()
-constexpr int64_t kStSeamPos = ((int64_t)(kStMaxRows + 1) * kStPairBytes + 15) & ~(int64_t)15;
-constexpr int64_t kStSeamPerWarp =
-    2 * align256(kStSeamPos + (int64_t)(kStMaxRows / kRescaleRows + 2) * 8);
+// seam scratch of one warp: the kernel's own layout (seam_bytes_per_warp, with
+// its slack for whole-warp stores past the last row) for the widest seam entry
+// the FP32 sweep could use, so that a change of the cell size or the slack
+// cannot let a warp write past the array
+constexpr int64_t kStSeamPerWarp = seam_bytes_per_warp(kStPairBytes, kStMaxRows);
+static_assert(kStPairBytes >= 4, "FP32 seam cells are 4 bytes");
+static_assert(kStSeamPerWarp % 256 == 0, "per-warp seam scratch keeps 256-byte alignment");
 
 constexpr int64_t kStFlagsOff = 0;                                                // counter, error flags
 constexpr int64_t kStKeysOff = 256;                                               // 2 x u64 per read
@@ -38,6 +41,8 @@ constexpr int64_t kStTasksOff = align256(kStKeysOff + 16 * (int64_t)kStMaxReads)
 constexpr int64_t kStNsampOff = align256(kStTasksOff + 32 * (int64_t)kStMaxReads); // int32 per read
 constexpr int64_t kStSeamOff = align256(kStNsampOff + 4 * (int64_t)kStMaxReads);
 constexpr int64_t kStBytes = kStSeamOff + kStSeamPerWarp * kStWarps * kStCtas;     // about 9 MiB
+static_assert(kStSeamOff + seam_bytes_per_warp(4, kStMaxRows) * kStWarps * kStCtas <= kStBytes,
+              "every warp's seam columns fit in the static scratch");
 
 // The scratch itself.  Host code must never pass this name to a kernel: on the
 // host it is only a stand-in symbol, not a device address.  The device address
@@ -76,6 +81,10 @@ extern "C" int dtwx_distances_static(const void *d_ref_pairs, int64_t ref_len, c
                                      dtwx_result *d_out, void *stream) {
   if (n_reads < 0 || ref_len <= 0 || !offsets || (n_reads > 0 && (!d_ref_pairs || !d_query || !d_out)))
     return st_fail(DTWX_E_ARG, "dtwx_distances_static: bad arguments");
+  if ((reinterpret_cast<uintptr_t>(d_ref_pairs) & 15) != 0)
+    return st_fail(DTWX_E_ARG, "dtwx_distances_static: d_ref_pairs must be 16-byte aligned");
+  if ((reinterpret_cast<uintptr_t>(d_out) & 7) != 0)
+    return st_fail(DTWX_E_ARG, "dtwx_distances_static: d_out must be 8-byte aligned");
   if (n_reads > kStMaxReads)
     return st_fail(DTWX_E_CAPACITY, "dtwx_distances_static: more than 4096 reads in one call");
   if (ref_len >= ((int64_t)1 << 32)) return st_fail(DTWX_E_CAPACITY, "dtwx_distances_static: reference too long");
@@ -123,7 +132,7 @@ extern "C" int dtwx_distances_static(const void *d_ref_pairs, int64_t ref_len, c
   if ((e = cudaMemcpyAsync(d_nsamp, h_nsamp, sizeof(int32_t) * n_reads, cudaMemcpyHostToDevice, st)) !=
       cudaSuccess)
     return st_fail(DTWX_E_CUDA, cudaGetErrorString(e));
-  if ((e = launch_reset(keys, 2 * n_reads, flags, st)) != cudaSuccess)
+  if ((e = launch_reset(keys, 2 * n_reads, flags, flags + 4, st)) != cudaSuccess)
     return st_fail(DTWX_E_CUDA, cudaGetErrorString(e));
   if (n_tasks) {
     SdtwParams p{};
@@ -154,7 +163,7 @@ extern "C" int dtwx_distances_static(const void *d_ref_pairs, int64_t ref_len, c
     if ((e = launch_sdtw(1, kStCells, kStWarps, kStCtas, p, nullptr, st)) != cudaSuccess)
       return st_fail(DTWX_E_CUDA, cudaGetErrorString(e));
   }
-  if ((e = launch_finalize(keys, d_nsamp, n_reads, 0, ref_len, threshold, d_out, st)) != cudaSuccess)
+  if ((e = launch_finalize(keys, d_nsamp, n_reads, 0, ref_len, threshold, flags + 4, d_out, st)) != cudaSuccess)
     return st_fail(DTWX_E_CUDA, cudaGetErrorString(e));
   return DTWX_OK;
 }

@@ -88,17 +88,26 @@ typedef struct dtwx_config {
   int32_t reserved[4];
 } dtwx_config;
 
+/* dtwx_result.call of every read of a call whose kernels reported a device
+ * error (a bounded wait gave up, or a task exceeded the scratch it was given):
+ * the sweep did not finish, the scores are NaN and `strand` holds the device
+ * error bits (1: a wait gave up, 2: a task was refused).  Device-pointer calls
+ * return before their kernels run, so this mark, and dtwx_sync, are how their
+ * callers learn of such an error. */
+#define DTWX_CALL_DEVICE_ERROR (-2)
+
 /* Per-read outcome.  end_pos is the DP column (0-based k-mer position on the
  * chosen strand's own 5'->3' axis) where the best alignment ends; score is
  * min(score_fwd, score_rev) with ties going to the smaller end column, then to
- * the forward strand.  n_samples = 0 marks a read that was skipped. */
+ * the forward strand.  n_samples = 0 marks a read that was skipped; call =
+ * DTWX_CALL_DEVICE_ERROR a read whose call hit a device error. */
 typedef struct dtwx_result {
   float score;
   float score_fwd;
   float score_rev;
   int32_t strand; /* 0 forward, 1 reverse complement */
   int64_t end_pos;
-  int32_t call;   /* 1 target, 0 non-target, -1 skipped */
+  int32_t call;   /* 1 target, 0 non-target, -1 skipped, DTWX_CALL_DEVICE_ERROR */
   int32_t n_samples;
 } dtwx_result;
 
@@ -174,15 +183,38 @@ int dtwx_classify_batch_i16(dtwx_handle *h, const int16_t *raw, const int64_t *o
  * Work is enqueued on `stream` (a cudaStream_t; 0 is the legacy default
  * stream, as for the reference's launcher) and the call returns without
  * synchronising.  Scratch (work queue, seam columns, keys) is owned by the
- * handle, so calls on one handle must not overlap on different streams. */
+ * handle, so calls on one handle must not overlap on different streams.
+ * Device-side errors surface in the results (DTWX_CALL_DEVICE_ERROR) and
+ * through dtwx_sync.  (The reference's launcher checks nothing.) */
 int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets,
                    int32_t n_reads, dtwx_result *d_out, void *stream);
 
 /* Device-resident variant of dtwx_classify_batch: raw FP32 samples already on
  * the device (d_raw, offsets on the host), results to d_out on `stream`.
- * Runs the window + z-score kernel, the sDTW kernel and the finalize kernel. */
+ * Runs the window + z-score kernel, the sDTW kernel and the finalize kernel.
+ * Device-side errors surface as for dtwx_distances. */
 int dtwx_classify_device(dtwx_handle *h, const float *d_raw, const int64_t *offsets,
                          int32_t n_reads, dtwx_result *d_out, void *stream);
+
+/* Wait for the kernels of the handle's most recent dtwx_distances or
+ * dtwx_classify_device call and return their device-side status: DTWX_OK,
+ * DTWX_E_TIMEOUT (a bounded wait gave up) or DTWX_E_CAPACITY (a task exceeded
+ * its scratch).  The status is reported once; DTWX_OK when no such call is
+ * outstanding.  The host-buffer entry points check the same status before
+ * they return.  Replaces the CUDA error check after the reference's launches
+ * (CUERR, src/include/hpc_helpers.hpp:103-113). */
+int dtwx_sync(dtwx_handle *h);
+
+/* Test hook for the bounded device waits.  The next sweep launch of this
+ * handle does not issue the first reference-strip copy of work item `item`
+ * (its queue ticket), so the warp that takes that item waits for data that
+ * never comes; every wait of that launch gives up after `spin_limit` polls
+ * (0 = the library's limit of 2^18 polls, about one second).  The warp then flags the error and
+ * leaves with no copy in flight, the call's results carry
+ * DTWX_CALL_DEVICE_ERROR and the status is DTWX_E_TIMEOUT.  One-shot: later
+ * launches are unaffected.  Applies to TMA-staged sweeps (the NO_REF_DEL
+ * kernels).  No reference counterpart (the reference has no bounded waits). */
+int dtwx_debug_stall_next(dtwx_handle *h, int32_t item, uint32_t spin_limit);
 
 /* FP32 sDTW of device-resident reads with no device allocation at all.
  * No counterpart in the reference.  For callers that cannot call cudaMalloc:
@@ -191,9 +223,10 @@ int dtwx_classify_device(dtwx_handle *h, const float *d_raw, const int64_t *offs
  * cannot absorb the device-wide synchronisation cudaMalloc/cudaFree may cause.
  * No handle is needed: the caller passes the z-scored reference as FP32 pairs
  * (fwd, rev) per k-mer column in device memory it owns -- ref_len columns,
- * readable up to the next multiple of 512 columns -- the z-scored reads
+ * readable up to the next multiple of 512 columns, 16-byte aligned (the sweep
+ * reads it in 16-byte loads; DTWX_E_ARG otherwise) -- the z-scored reads
  * (d_query on the device, offsets on the host) and d_out (n_reads results on
- * the device).  Scratch (task table, work counter, seam columns, result keys)
+ * the device, 8-byte aligned).  Scratch (task table, work counter, seam columns, result keys)
  * is one static device array of about 9 MiB that every GPU loading the library
  * keeps until the process exits.  Limits: at most 4096 reads per call and 2048
  * samples per read; larger requests return DTWX_E_CAPACITY with a message in
@@ -201,7 +234,9 @@ int dtwx_classify_device(dtwx_handle *h, const float *d_raw, const int64_t *offs
  * device address (cudaGetSymbolAddress); make that first call before any
  * stream capture.  All calls share the array, so calls that overlap on the GPU
  * (different streams, or several host threads) race and must be serialised by
- * the caller.  Asynchronous on `stream` (0 = legacy default stream). */
+ * the caller.  Asynchronous on `stream` (0 = legacy default stream).  A device
+ * error of the call (a task the scratch cannot hold) marks every result with
+ * DTWX_CALL_DEVICE_ERROR. */
 int dtwx_distances_static(const void *d_ref_pairs, int64_t ref_len, const float *d_query,
                           const int64_t *offsets, int32_t n_reads, float threshold,
                           dtwx_result *d_out, void *stream);

@@ -7,9 +7,12 @@ free may cause.  Its scratch is one static device array inside the library.
 
 Checked here through the C ABI: two calls in a row return what the regular
 device entry point (dtwx_distances, handle-owned scratch) returns for the same
-reads, within the FP32 tolerance of the other GPU tests, and requests beyond
-the array's limits are refused with DTWX_E_CAPACITY.  This file is collected
-last so that a failure here does not hide any other test.
+reads, within the FP32 tolerance of the other GPU tests, and what the FP64
+oracle gives for the same z-scored reads and reference (1e-5 relative, exact
+end columns); no result carries the device-error mark; requests beyond the
+array's limits are refused with DTWX_E_CAPACITY, and misaligned buffers with
+DTWX_E_ARG.  This file is collected last so that a failure here does not hide
+any other test.
 """
 import ctypes
 
@@ -30,7 +33,7 @@ def _pairs(fwd, rev):
     return pairs
 
 
-def test_static_scratch_matches_regular_entry(built_lib):
+def test_static_scratch_matches_regular_entry(built_lib, oracle):
     import torch
     import dtwax_gb300 as d
     from dtwax_gb300 import synth
@@ -67,6 +70,17 @@ def test_static_scratch_matches_regular_entry(built_lib):
 
     want = res[0]
     assert want["call"][-1] == -1  # the empty read
+    # the FP64 oracle on the very inputs the GPU saw (FP32 reference, FP32 reads)
+    sf, ef, sr, er = oracle.sdtw_batch(fwd.astype(np.float64), rev.astype(np.float64),
+                                       np.concatenate(zs).astype(np.float64), offsets)
+    live = want["n_samples"] > 0
+    for got in res[1:]:
+        assert (got["call"] != d.CALL_DEVICE_ERROR).all()
+        np.testing.assert_allclose(got["score_fwd"][live], sf[live], rtol=FP32_RTOL)
+        np.testing.assert_allclose(got["score_rev"][live], sr[live], rtol=FP32_RTOL)
+        score, end, strand = oracle.combine(sf, ef, sr, er)
+        np.testing.assert_array_equal(got["end_pos"][live], end[live])
+        np.testing.assert_array_equal(got["strand"][live], strand[live])
     for got in res[1:]:
         np.testing.assert_allclose(got["score_fwd"], want["score_fwd"], rtol=FP32_RTOL)
         np.testing.assert_allclose(got["score_rev"], want["score_rev"], rtol=FP32_RTOL)
@@ -99,4 +113,11 @@ def test_static_scratch_refuses_oversized_requests(built_lib):
                                    ctypes.c_void_p(d_out.data_ptr()), None)
     assert rc == -7
     assert b"2048" in lib.dtwx_last_error(None)
+
+    one = np.array([0, 100], np.int64)
+    rc = lib.dtwx_distances_static(ctypes.c_void_p(d_ref.data_ptr() + 8), 1000, ctypes.c_void_p(d_q.data_ptr()),
+                                   one.ctypes.data_as(i64p), 1, ctypes.c_float(1.0),
+                                   ctypes.c_void_p(d_out.data_ptr()), None)
+    assert rc == -1  # DTWX_E_ARG: the reference pairs are read in 16-byte loads
+    assert b"16-byte" in lib.dtwx_last_error(None)
     torch.cuda.synchronize()
