@@ -33,17 +33,27 @@
 // src/ReadUntil/simulate_minion.py or ont_readuntil.py):
 //
 //   dtwx_main --fifo <kmer_model> <ref.fasta> <pipe> [--fp32|--mixed] [--ref-del] [--threshold T]
-//             [--reads N] [--query-len N]
+//             [--reads N] [--query-len N] [--batches N]
 //
 // reads batches of N (default 10) reads x query-len (default 2,048) unsigned
 // 8-bit samples from the named pipe (generate_load_squiggle.hpp:303-343,
 // PIPE_SIZE = 10 x 2,048 at ru_main.cu:131-132) and prints, per read and with no
 // header, the line the reference prints (ru_main.cu:304-310):
 //   <idx>\t<idx>\t<QUERY_LEN>\t<REF_LEN>\t<fwd>\t<rev>
-// flushing after every batch.  It stops at the end of the stream (the reference
-// loops forever); a partial last batch is dropped, as the reference only
-// processes whole batches.
+// flushing after every batch.  The reference's writers open the pipe, write
+// part of a batch and close it again (ont_readuntil.py:49-50 writes 16,000
+// bytes per open; simulate_minion.py reopens in its loop), and its reader
+// reopens the pipe for every batch (generate_load_squiggle.hpp:94-106 inside
+// the while (true) of ru_main.cu:172-179).  So here a writer closing the pipe
+// ends nothing: the reader reopens it and keeps filling the current batch from
+// the next writer.  Like the reference it runs until it is stopped: SIGINT or
+// SIGTERM ends it cleanly between reads (exit status 0), and --batches N stops
+// it after N whole batches.  Bytes of an unfinished batch are dropped.
 #include <dirent.h>
+#include <errno.h>
+#include <fcntl.h>
+#include <signal.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cstdio>
@@ -172,13 +182,17 @@ bool load_txt(const std::string &path, std::vector<float> &out, std::string &err
   return true;
 }
 
+volatile sig_atomic_t g_fifo_stop = 0;
+void fifo_on_signal(int) { g_fifo_stop = 1; }
+
 // The Read Until FIFO loop (see the header comment).
 int run_fifo(int argc, char **argv) {
   if (argc < 5) {
     std::cerr << "usage: dtwx_main --fifo <kmer_model> <ref.fasta> <pipe> [--fp32|--mixed] [--ref-del]\n"
-                 "       [--threshold T] [--reads N] [--query-len N]\n";
+                 "       [--threshold T] [--reads N] [--query-len N] [--batches N]\n";
     return 2;
   }
+  long max_batches = 0;
   const std::string model = argv[2], fasta = argv[3], pipe_path = argv[4];
   dtwx_config cfg;
   dtwx_config_default(&cfg);
@@ -204,12 +218,14 @@ int run_fifo(int argc, char **argv) {
       n_reads = atoi(next());
     else if (a == "--query-len")
       qlen = atoi(next());
+    else if (a == "--batches")
+      max_batches = atol(next());
     else {
       std::cerr << "unknown option " << a << "\n";
       return 2;
     }
   }
-  if (n_reads <= 0 || qlen <= 0) {
+  if (n_reads <= 0 || qlen <= 0 || max_batches < 0) {
     std::cerr << "--reads and --query-len must be positive\n";
     return 2;
   }
@@ -219,12 +235,13 @@ int run_fifo(int argc, char **argv) {
     return 1;
   }
   const int64_t ref_len = dtwx_ref_len(h);
-  std::ifstream pipe(pipe_path, std::ios::binary);
-  if (!pipe) {
-    std::cerr << "cannot open " << pipe_path << "\n";
-    dtwx_destroy(h);
-    return 1;
-  }
+  // no SA_RESTART: a signal interrupts a blocked open() or read() (EINTR)
+  struct sigaction sa;
+  memset(&sa, 0, sizeof(sa));
+  sa.sa_handler = fifo_on_signal;
+  sigemptyset(&sa.sa_mask);
+  sigaction(SIGINT, &sa, nullptr);
+  sigaction(SIGTERM, &sa, nullptr);
   const size_t batch = (size_t)n_reads * (size_t)qlen;
   std::vector<char> buf(batch);
   std::vector<float> raw(batch);
@@ -232,7 +249,36 @@ int run_fifo(int argc, char **argv) {
   for (int r = 0; r <= n_reads; ++r) offsets[r] = (int64_t)r * qlen;
   std::vector<dtwx_result> res((size_t)n_reads);
   int rc = 0;
-  while (pipe.read(buf.data(), (std::streamsize)batch) && (size_t)pipe.gcount() == batch) {
+  int fd = -1;
+  size_t have = 0;
+  long batches = 0;
+  while (!g_fifo_stop) {
+    if (fd < 0) {
+      // blocks until a writer opens the pipe
+      fd = open(pipe_path.c_str(), O_RDONLY);
+      if (fd < 0) {
+        if (errno == EINTR) continue;
+        std::cerr << "cannot open " << pipe_path << ": " << strerror(errno) << "\n";
+        rc = 1;
+        break;
+      }
+    }
+    const ssize_t k = read(fd, buf.data() + have, batch - have);
+    if (k < 0) {
+      if (errno == EINTR) continue;
+      std::cerr << "read " << pipe_path << ": " << strerror(errno) << "\n";
+      rc = 1;
+      break;
+    }
+    if (k == 0) {
+      // the writer closed the pipe: wait for the next one, keep the batch
+      close(fd);
+      fd = -1;
+      continue;
+    }
+    have += (size_t)k;
+    if (have < batch) continue;
+    have = 0;
     for (size_t i = 0; i < batch; ++i) raw[i] = (float)(unsigned char)buf[i];
     if (dtwx_classify_batch(h, raw.data(), offsets.data(), n_reads, res.data()) != DTWX_OK) {
       std::cerr << "dtwx_classify_batch: " << dtwx_last_error(h) << "\n";
@@ -243,7 +289,9 @@ int run_fifo(int argc, char **argv) {
       std::cout << j << "\t" << j << "\t" << qlen << "\t" << ref_len << "\t" << res[j].score_fwd << "\t"
                 << res[j].score_rev << "\n";
     std::cout.flush();
+    if (max_batches && ++batches >= max_batches) break;
   }
+  if (fd >= 0) close(fd);
   dtwx_destroy(h);
   return rc;
 }

@@ -413,34 +413,45 @@ def test_cli_drop_in(lib, kat, tmp_path):
         np.testing.assert_allclose([float(r[4]) for r in rows], res["score_fwd"], rtol=rtol)
 
 
+def _fifo_write_session(fifo, payload, proc, timeout=120):
+    """One writer session as the reference's Read Until scripts do it: open the
+    pipe, write, close (ont_readuntil.py:49-50).  The open is retried without
+    blocking until the reader has (re)opened its end."""
+    import os
+    import time
+    fd = None
+    t0 = time.time()
+    while fd is None and time.time() - t0 < timeout and proc.poll() is None:
+        try:
+            fd = os.open(fifo, os.O_WRONLY | os.O_NONBLOCK)
+        except OSError:
+            time.sleep(0.05)
+    assert fd is not None, proc.stderr.read() if proc.poll() is not None else "reader never opened the pipe"
+    os.set_blocking(fd, True)
+    os.write(fd, payload)
+    os.close(fd)
+
+
 def test_cli_read_until_fifo(lib, kat, tmp_path):
     """`dtwx_main --fifo <kmer_model> <ref.fasta> <pipe>`: the reference's Read
     Until binary protocol (ru_main.cu, generate_load_squiggle.hpp:303-343).
     Batches of 10 reads x 2,048 uint8 samples arrive on a named pipe, and one
-    6-token line per read comes back with the scores of dtwx_classify_batch."""
+    6-token line per read comes back with the scores of dtwx_classify_batch.
+    The writers open, write and close the pipe per session, as
+    ont_readuntil.py does (16,000 bytes per open): the first batch is split
+    across two sessions, and the reader keeps filling it across the reopen."""
     import os
-    import time
     import dtwax_gb300 as d
     fasta, model = write_kat_files(kat, str(tmp_path))
     fifo = str(tmp_path / "pipe")
     os.mkfifo(fifo)
     rng = np.random.default_rng(9)
-    data = rng.integers(0, 256, size=2 * 10 * 2048, dtype=np.uint8)
-    proc = subprocess.Popen([d.CLI_PATH, "--fifo", model, fasta, fifo], stdout=subprocess.PIPE,
+    data = rng.integers(0, 256, size=2 * 10 * 2048, dtype=np.uint8).tobytes()
+    proc = subprocess.Popen([d.CLI_PATH, "--fifo", model, fasta, fifo, "--batches", "2"], stdout=subprocess.PIPE,
                             stderr=subprocess.PIPE, text=True)
     try:
-        # open for writing without blocking: wait (bounded) until the reader has opened the pipe
-        fd = None
-        t0 = time.time()
-        while fd is None and time.time() - t0 < 120 and proc.poll() is None:
-            try:
-                fd = os.open(fifo, os.O_WRONLY | os.O_NONBLOCK)
-            except OSError:
-                time.sleep(0.05)
-        assert fd is not None, proc.stderr.read() if proc.poll() is not None else "reader never opened the pipe"
-        os.set_blocking(fd, True)
-        os.write(fd, data.tobytes() + b"\x00" * 100)  # two whole batches and a partial one (dropped)
-        os.close(fd)
+        _fifo_write_session(fifo, data[:16000], proc)   # part of batch 1, then the writer closes
+        _fifo_write_session(fifo, data[16000:], proc)   # the rest of batch 1 and batch 2
         out, err = proc.communicate(timeout=120)
     finally:
         if proc.poll() is None:
@@ -450,11 +461,45 @@ def test_cli_read_until_fifo(lib, kat, tmp_path):
     assert len(rows) == 20 and all(len(r) == 6 for r in rows)
     assert [r[0] for r in rows] == [str(j) for j in range(10)] * 2
     with d.Classifier(fasta=fasta, kmer_model=model) as clf:
-        x = data.astype(np.float32)
+        x = np.frombuffer(data, np.uint8).astype(np.float32)
         res = clf.classify(raw=x, offsets=np.arange(21, dtype=np.int64) * 2048)
         assert all(r[3] == str(clf.ref_len) for r in rows)
     np.testing.assert_allclose([float(r[4]) for r in rows], res["score_fwd"], rtol=1e-5)
     np.testing.assert_allclose([float(r[5]) for r in rows], res["score_rev"], rtol=1e-5)
+
+
+def test_cli_read_until_fifo_runs_until_signalled(lib, kat, tmp_path):
+    """Without --batches the FIFO reader runs like the reference's (while
+    (true), ru_main.cu:172): writers may come and go; SIGTERM ends it with
+    status 0 after the batches it has printed."""
+    import os
+    import signal
+    import time
+    import dtwax_gb300 as d
+    fasta, model = write_kat_files(kat, str(tmp_path))
+    fifo = str(tmp_path / "pipe")
+    os.mkfifo(fifo)
+    data = np.random.default_rng(10).integers(0, 256, size=10 * 2048, dtype=np.uint8).tobytes()
+    proc = subprocess.Popen([d.CLI_PATH, "--fifo", model, fasta, fifo], stdout=subprocess.PIPE,
+                            stderr=subprocess.PIPE, text=True)
+    try:
+        _fifo_write_session(fifo, data, proc)
+        lines = []
+        t0 = time.time()
+        while len(lines) < 10 and time.time() - t0 < 120 and proc.poll() is None:
+            line = proc.stdout.readline()
+            if line:
+                lines.append(line)
+        assert len(lines) == 10
+        time.sleep(0.2)  # the reader is back in open(), waiting for the next writer
+        assert proc.poll() is None
+        proc.send_signal(signal.SIGTERM)
+        out, err = proc.communicate(timeout=60)
+    finally:
+        if proc.poll() is None:
+            proc.kill()
+    assert proc.returncode == 0, err
+    assert out == ""
 
 
 def test_autotune_picks_a_compiled_shape_and_keeps_results(lib, genome_pair):
