@@ -1,10 +1,13 @@
-"""Benchmark of the sDTW classification path on the precision-study workload.
+"""Benchmark of the sDTW classification path on the batched uneven-read workload.
 
-Workload (one step): 2,048 reads x 2,000 samples against a seeded random 1 Mb
-genome (999,995 k-mer columns per strand, both strands), i.e. 8.19e12 DP
-cells: raw pA samples resident in HBM -> window + z-score kernel -> sDTW sweep
-(FP16 half2 cells, FP32 offsets) -> min/argmin finalize.  Metric: sDTW GCUPS
-= sum over reads of samples x columns x 2 strands / s / 1e9.
+Workload (one step, default C3): 8,192 reads of U[1000, 8000] samples (50/50
+target / non-target) against a seeded random 5 Mb genome (4,999,995 k-mer
+columns per strand, both strands), about 3.7e14 DP cells in one persistent
+launch: raw pA samples resident in HBM -> window + z-score kernel -> sDTW sweep
+(FP16 half2 cells, FP32 offsets) -> min/argmin finalize, replayed as a captured
+CUDA graph with the autotuned launch shape.  --workload C2 runs the
+precision-study shape (2,048 x 2,000 samples vs 1 Mb).  Metric: sDTW GCUPS =
+sum over reads of samples x columns x 2 strands / s / 1e9.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -25,7 +28,6 @@ from __future__ import annotations
 import argparse
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -37,7 +39,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = "C2"
+WORKLOAD = "C3"
 WORKLOAD_DESC = {
     "C2": ("precision-study shape: seeded random 1 Mb genome (999,995 k-mer columns per strand, both strands), "
            "2,048 reads x 2,000 samples (1,024 target / 1,024 non-target), dwell geometric mean 9, noise sd 1.8 pA"),
@@ -118,46 +120,63 @@ def measured_hbm_gbs():
         return None
 
 
-def traffic_from_profile(precision: str, workload: str):
-    """DRAM bytes per sweep launch from the committed ncu summary of this
-    precision and workload, if present."""
-    path = os.path.join(ROOT, "profiles", f"sdtw_{precision}_{workload}.md")
-    if not os.path.exists(path):
+def traffic_per_launch(precision: str, workload: str):
+    """DRAM bytes per sweep launch of this precision and workload from
+    profiles/traffic.json (ncu dram__bytes_read.sum + dram__bytes_write.sum,
+    written beside the summary each figure comes from), or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        rec = json.load(open(path)).get(f"sdtw_{precision}_{workload}")
+    except (OSError, ValueError):
         return None
-    m = re.search(r"dram_bytes_per_full_launch\s*=\s*([0-9.eE+]+)", open(path).read())
-    return float(m.group(1)) if m else None
+    return float(rec["dram_bytes_per_launch"]) if rec else None
 
 
 def cpu_baseline(workload, n_steps: int = 1, target_s: float = CPU_TARGET_S):
-    """FP64 OpenMP oracle (restatement of sdtw.py `sdtw_default`) on a read
-    sample of the same workload, all host threads.  Returns the record."""
+    """FP64 OpenMP oracle (restatement of sdtw.py `sdtw_default`) on a
+    bounded sample of the same workload, all host threads.  The sample is one
+    read per thread (more when they are short), each aligned over a prefix of
+    its samples against both strands of the whole reference, the prefix
+    sized so that a pass takes about target_s.  Returns the record."""
     from oracle import oracle as O
 
     O.build()
     fwd, rev = O.build_levels(workload.genome, workload.table.astype(np.float64))
     m = fwd.size
     reads = workload.reads
-    zs = [O.zscore(reads.read(i).astype(np.float64), 1e-4) for i in range(reads.n)]
     cores = O.max_threads()
+    lens = np.diff(reads.offsets)
+    zs = {}
 
-    def run(idx):
-        q = np.concatenate([zs[i] for i in idx])
-        offs = np.concatenate([[0], np.cumsum([zs[i].size for i in idx])]).astype(np.int64)
+    def z(i):
+        if i not in zs:
+            zs[i] = O.zscore(reads.read(i).astype(np.float64), 1e-4)
+        return zs[i]
+
+    def run(idx, prefix):
+        qs = [z(i)[:prefix] for i in idx]
+        q = np.concatenate(qs)
+        offs = np.concatenate([[0], np.cumsum([x.size for x in qs])]).astype(np.int64)
         t = time.perf_counter()
         O.sdtw_batch(fwd, rev, q, offs)
         dt = time.perf_counter() - t
-        cells = float(sum(zs[i].size for i in idx)) * m * 2
-        return cells, dt
+        return float(q.size) * m * 2, dt
 
-    # calibrate on one read per core, then size the sample to about target_s
-    c0, t0 = run(list(range(min(cores, reads.n))))
+    # calibrate on one read per thread over a short prefix, then size the
+    # sample (reads x prefix) to about target_s per pass
+    idx = list(range(min(cores, reads.n)))
+    c0, t0 = run(idx, 64)
     rate = c0 / t0
-    per_read = float(zs[0].size) * m * 2
-    n = int(max(cores, min(reads.n, round(target_s * rate / per_read / cores) * cores)))
-    n = min(n, reads.n)
+    want = target_s * rate / (m * 2)              # samples per pass
+    n = len(idx)
+    prefix = int(min(lens[idx].min(), max(64, want / n)))
+    if prefix >= lens[idx].min() and want > n * prefix:  # whole reads: take more of them
+        n = int(min(reads.n, max(n, round(want / lens.mean() / cores) * cores)))
+        idx = list(range(n))
+        prefix = int(lens.max())
     total_c, total_t = 0.0, 0.0
     for _ in range(n_steps):
-        c, t = run(list(range(n)))
+        c, t = run(idx, prefix)
         total_c += c
         total_t += t
     # the reference's Python sDTW (scripts/sdtw.py sdtw_default) needs numba; its
@@ -167,14 +186,18 @@ def cpu_baseline(workload, n_steps: int = 1, target_s: float = CPU_TARGET_S):
         numba_state = "installed but not timed (the oracle port is the timed baseline)"
     except ImportError:
         numba_state = "unavailable: numba is not installed"
-    q1 = zs[0][:200]
+    q1 = z(0)[:200]
     t = time.perf_counter()
     O.np_sdtw(fwd, q1)
     np_dt = time.perf_counter() - t
+    whole = prefix >= lens[idx].max()
+    shape = "whole reads" if whole else f"the first {prefix} samples of each"
     return {"value": total_c / total_t / 1e9, "unit": "GCUPS", "cores": cores, "kind": "port",
-            "sample": f"{n} of {reads.n} reads x {zs[0].size} samples against both strands of the full "
+            "sample": f"{n} of {reads.n} reads ({shape}) against both strands of the full "
                       f"{m}-column reference, FP64, {n_steps} pass(es)",
-            "seconds": total_t, "reads_per_s": n * n_steps / total_t,
+            "seconds": total_t,
+            # reads/s of whole reads of the workload's mean length at the measured cell rate
+            "reads_per_s": total_c / total_t / (float(lens.mean()) * m * 2),
             "numpy_restatement_1core_gcups": float(q1.size) * m / np_dt / 1e9,
             "numba_original": numba_state}
 
@@ -199,10 +222,13 @@ def run_serving(name: str, precision: int, device: int, duration_s: float, batch
     tab = synth.level_table()
     cfg = readuntil.ServeConfig(channels=spec["channels"], duration_s=duration_s, warmup_s=2.0)
     reads = readuntil.make_pool(g, o, tab, cfg)
+    # accept / reject rates from reads that are never served: the call
+    # accuracy of the run is held out
+    held = readuntil.make_pool(g, o, tab, cfg, held_out=True, n=256)
     state_precision = d.STATE_FP16 if state == "fp16" and precision == d.FP16 else d.STATE_FP32
     with d.Classifier(sequence=g, level_table=tab, precision=precision, device=device,
                       serve_batches=batches, state_precision=state_precision) as clf:
-        accept, reject = readuntil.calibrate(clf, reads, cfg)
+        accept, reject = readuntil.calibrate(clf, held, cfg)
         rec = readuntil.run(clf, reads, cfg, accept, reject, state_budget_bytes=spec["budget_gb"] * 1e9)
     # row-state traffic of the resumed sweeps: a slot holds both strands' last
     # DP row (8 B per column pair in FP32, about 4 B with FP16 rows); each
@@ -210,6 +236,7 @@ def run_serving(name: str, precision: int, device: int, duration_s: float, batch
     slot_bytes = (4 if state_precision == d.STATE_FP16 else 8) * (spec["genome_len"] - 5)
     rec["row_state_gbs"] = rec["chunks_processed_per_s"] * 2 * slot_bytes / 1e9
     rec["row_state_bytes_per_chunk_step"] = 2 * slot_bytes
+    rec["calibration"] = "accept/reject rates from the first chunks of 256 held-out reads (not served)"
     rec["workload"] = (f"{name}: {spec['channels']} channels, 1,600-sample chunks every 0.4 s, Poisson read "
                        f"starts 1/s/channel, <= 3 chunks per decision, {spec['genome_len'] // 1_000_000} Mb "
                        f"seeded genome ({2 * (spec['genome_len'] - 5)} columns), row-state budget "
@@ -218,11 +245,12 @@ def run_serving(name: str, precision: int, device: int, duration_s: float, batch
     return rec
 
 
-REF_GPU_GEOMETRY = {"C2": "fp16_1000064"}
-REF_GPU_GEOMETRY_FP32 = {"C2": "fp32_2000128"}
+REF_GPU_GEOMETRY = {"C2": "fp16_1000064", "C3": "fp16_5000320"}
+REF_GPU_GEOMETRY_FP32 = {"C2": "fp32_2000128", "C3": "fp32_10000640"}
+REF_FP32_READS = {"C2": 4, "C3": 2}  # one read per launch: about 1 s (C2) and 10 s (C3) per read
 
 
-def reference_gpu_kernel(workload, n_reads: int = 2048, shipped_launches: int = 2, fp32_reads: int = 4):
+def reference_gpu_kernel(workload, n_reads: int = 2048, shipped_launches: int = 2, fp32_reads: int = 0):
     """The reference's own FP16 kernel (FullDTW::DTW, src/include/DTW.cu,
     compiled from its sources into oracle/_ref) on this GPU, on the workload's
     genome: reads of the kernel's fixed 2,048-sample query from the same
@@ -238,6 +266,7 @@ def reference_gpu_kernel(workload, n_reads: int = 2048, shipped_launches: int = 
     from oracle import oracle as O
     from oracle import ref_kernel as RK
 
+    fp32_reads = fp32_reads or REF_FP32_READS.get(workload.name, 2)
     name = REF_GPU_GEOMETRY.get(workload.name)
     if name is None:
         return {"unavailable": f"no reference-kernel geometry for {workload.name} (its query length is fixed "
@@ -261,7 +290,7 @@ def reference_gpu_kernel(workload, n_reads: int = 2048, shipped_launches: int = 
         d_ref = k.reference(fwd.astype(np.float32), rev.astype(np.float32))
         d_q = k.queries(z)
         d_dist = torch.empty(n_reads, dtype=torch.int32, device="cuda")
-        d_last = torch.empty(n_reads * k.ref_len, dtype=torch.int32, device="cuda")
+        d_last = torch.empty(min(n_reads, k.max_reads_per_launch()) * k.ref_len, dtype=torch.int32, device="cuda")
         stream = torch.cuda.current_stream()
         sh = stream.cuda_stream
         # warm-up: one small launch
@@ -279,14 +308,18 @@ def reference_gpu_kernel(workload, n_reads: int = 2048, shipped_launches: int = 
         nr = shipped_launches * RK.BLOCK_NUM
         out["as_shipped"] = {"value": nr * cells_per_read / (ms * 1e-3) / 1e9, "reads_per_s": nr / (ms * 1e-3),
                              "ms": ms, "launches": shipped_launches, "reads_per_launch": RK.BLOCK_NUM}
-        # every read in one launch (one warp per read, all resident)
+        # every read in one launch (one warp per read), or as many per launch
+        # as the kernel's 32-bit row-state index allows (429 on the 5 Mb genome)
+        per = min(n_reads, k.max_reads_per_launch())
         b.record(stream)
-        k.launch(d_ref, d_q, d_dist, d_last, n_reads, stream=sh)
+        for s0 in range(0, n_reads, per):
+            k.launch(d_ref, d_q, d_dist[s0:], d_last, min(per, n_reads - s0), first_read=s0, stream=sh)
         e.record(stream)
         torch.cuda.synchronize()
         ms = b.elapsed_time(e)
         out["one_launch"] = {"value": n_reads * cells_per_read / (ms * 1e-3) / 1e9,
-                             "reads_per_s": n_reads / (ms * 1e-3), "ms": ms, "reads": n_reads}
+                             "reads_per_s": n_reads / (ms * 1e-3), "ms": ms, "reads": n_reads,
+                             "reads_per_launch": per, "launches": -(-n_reads // per)}
     name32 = REF_GPU_GEOMETRY_FP32.get(workload.name)
     if name32 is None or not RK.available(name32):
         out["fp32_one_read_per_launch"] = {"unavailable": f"no FP32 reference-kernel cubin for {workload.name}"}
@@ -312,6 +345,9 @@ def reference_gpu_kernel(workload, n_reads: int = 2048, shipped_launches: int = 
                       f"{-(-2 * m // RK.TILE)} tiles",
             "value": fp32_reads * cells_per_read / (ms * 1e-3) / 1e9, "reads_per_s": fp32_reads / (ms * 1e-3),
             "ms": ms, "reads": fp32_reads, "launches": fp32_reads,
+            # the same cell rate in reads of the workload's own mean length
+            "reads_per_s_at_workload_mean_length": fp32_reads * cells_per_read / (ms * 1e-3)
+            / (float(np.diff(workload.reads.offsets).mean()) * m * 2),
             "score_min": float(d_dist.min().item()), "score_max": float(d_dist.max().item())}
     return out
 
@@ -343,6 +379,43 @@ def run_reference(args, rank, world):
             line["reference_gpu_kernel"] = {"unavailable": f"{type(exc).__name__}: {exc}"}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def c2_subrecord(device: int, precision: int, peak_cells_s: float, steps: int = 5, warmup: int = 3):
+    """The precision-study shape (C2: 2,048 x 2,000 samples vs 1 Mb) beside a
+    C3 line: the same device-resident step, timed the same way."""
+    import torch
+    import dtwax_gb300 as d
+    from dtwax_gb300 import synth
+
+    w = synth.make_workload("C2")
+    cells = w.cells()
+    with d.Classifier(sequence=w.genome, level_table=w.table, precision=precision, device=device) as clf:
+        stream = torch.cuda.Stream()
+        d_raw = torch.tensor(w.reads.raw, device="cuda")
+        d_out = torch.zeros(32 * w.reads.n, dtype=torch.uint8, device="cuda")
+        flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+        step_ms, sweep_ms = [], []
+        with torch.cuda.stream(stream):
+            for i in range(warmup + steps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                clf.classify_device(d_raw.data_ptr(), w.reads.offsets, d_out.data_ptr(), stream.cuda_stream)
+                e1.record(stream)
+                stream.synchronize()
+                if i >= warmup:
+                    step_ms.append(e0.elapsed_time(e1))
+                    sweep_ms.append(clf.last_sweep_ms())
+        clf.sync()
+        tuning = clf.tuning()
+    sweep = cells / (float(np.mean(sweep_ms)) / 1e3) / 1e9
+    return {"workload": f"C2: {WORKLOAD_DESC['C2']}", "steps": steps, "warmup": warmup,
+            "value": cells * steps / (sum(step_ms) / 1e3) / 1e9, "unit": "GCUPS",
+            "reads_per_s": w.reads.n * steps / (sum(step_ms) / 1e3), "ms_per_step": sum(step_ms) / steps,
+            "sweep_gcups": sweep, "sweep_frac_of_probe": sweep / (peak_cells_s / 1e9),
+            "traffic": traffic_per_launch({d.FP16: "fp16", d.FP32: "fp32", d.MIXED: "mixed"}[precision], "C2"),
+            "tuning": tuning}
 
 
 def run_ours(args, rank, world, local):
@@ -406,21 +479,26 @@ def run_ours(args, rank, world, local):
             flush.zero_()  # L2 flush between timed steps, outside the events
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.nvtx.range_push("timed_step")  # lets ncu pick a timed launch (--nvtx-include)
             e0.record(stream)
             step()
             e1.record(stream)
+            torch.cuda.nvtx.range_pop()
             stream.synchronize()
             step_ms.append(e0.elapsed_time(e1))
             sweep_ms.append(clf.last_sweep_ms())
     barrier()
     clock_rec = clocks.stop()
+    clf.sync()  # raises if a kernel of the timed steps reported a device-side error
     tuning = clf.tuning()
     total_ms = max_over_ranks(sum(step_ms))
     res = np.frombuffer(d_out.cpu().numpy().tobytes(), d.RESULT_DTYPE)
+    if (res["call"] < 0).any():
+        raise SystemExit(f"{int((res['call'] < 0).sum())} reads have no valid result")
 
     # end to end through the public host API: host samples in, results out
     e2e_ms = []
-    for _ in range(max(1 if args.workload == "C3" else 2, min(args.steps, 5))):
+    for _ in range(1 if args.workload == "C3" else max(2, min(args.steps, 5))):
         t = time.perf_counter()
         host_res = clf.classify(raw=w.reads.raw, offsets=w.reads.offsets)
         e2e_ms.append((time.perf_counter() - t) * 1e3)
@@ -440,6 +518,7 @@ def run_ours(args, rank, world, local):
         plain_s = time.perf_counter() - t
         plain_shape = pclf.tuning()
     plain_rps = n_plain / plain_s
+    plain_gcups = float(w.reads.offsets[n_plain]) * w.ref_len * 2 / plain_s / 1e9
 
     value = world * cells * args.steps / (total_ms / 1e3) / 1e9
     reads_per_s = world * n_reads * args.steps / (total_ms / 1e3)
@@ -458,7 +537,7 @@ def run_ours(args, rank, world, local):
         # HFMA2), its HSUB2 and HFMA2 holding the FMA pipe 2 cycles each
         per_sm_cycle = 128.0 / 4.0 if precision == d.FP32 else 64.0
     theoretical = sms * per_sm_cycle * mhz * 1e6 / 1e9
-    traffic = traffic_from_profile(args.precision, args.workload) if not ref_del else None
+    traffic = traffic_per_launch(args.precision, args.workload) if not ref_del else None
     # the roofline peak: the measured probe of the cell's instruction mix where
     # it is a ceiling (FP16 and MIXED cells); the FP32 probe runs below the
     # sweep itself and REF_DEL has a different mix, so those use the bound
@@ -499,13 +578,19 @@ def run_ours(args, rank, world, local):
                 "path": "dtwx_classify_batch (host raw samples -> host results)"},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clock_rec,
-        "plain_fp32": {"reads_per_s": plain_rps, "sample_reads": n_plain, "tuning": plain_shape,
-                       "speedup_reads_per_s": reads_per_s / world / plain_rps},
+        "plain_fp32": {"reads_per_s": plain_rps, "gcups": plain_gcups, "sample_reads": n_plain,
+                       "sample_mean_samples": float(w.reads.offsets[n_plain]) / n_plain, "tuning": plain_shape,
+                       "path": "dtwx_classify_plain_fp32: this library's FP32 kernel, one launch per read, "
+                               "shape autotuned for one-read batches",
+                       "speedup_reads_per_s": reads_per_s / world / plain_rps,
+                       "speedup_gcups": value / world / plain_gcups},
         "check": {"target_score_per_sample_max": float((res["score"] / res["n_samples"])[t_mask].max()),
                   "other_score_per_sample_min": float((res["score"] / res["n_samples"])[~t_mask].min())},
     }
     # the serving run and the CPU baseline belong to the one-GPU line only: with
     # N ranks every GPU would be held while rank 0 alone ran them
+    if args.workload == "C3" and not args.no_c2 and not ref_del and not args.reads and rank == 0 and world == 1:
+        line["c2"] = c2_subrecord(local, precision, peak)
     if args.serving != "none" and rank == 0 and world == 1:
         line["serving"] = run_serving(args.serving, precision, local, args.serving_seconds, args.serve_batches,
                                       args.state)
@@ -542,7 +627,7 @@ def main():
                     help="reference arm: CPU seconds over all timed steps (each step is a bounded read sample)")
     ap.add_argument("--serving", choices=["none", "C4", "C5"], default="C4",
                     help="Read Until serving simulation reported beside the batch metric")
-    ap.add_argument("--serving-seconds", type=float, default=6.0)
+    ap.add_argument("--serving-seconds", type=float, default=30.0)
     ap.add_argument("--serve-batches", type=int, default=0, help="serving batches in flight (0 = library default)")
     ap.add_argument("--cells", type=int, default=0, help="cells per thread (0 = tuned)")
     ap.add_argument("--strips", type=int, default=0, help="strips per work item (0 = tuned)")
@@ -550,7 +635,8 @@ def main():
     ap.add_argument("--autotune", action="store_true", help="time candidate launch shapes before measuring")
     ap.add_argument("--graphs", action="store_true", help="replay the step as a captured CUDA graph")
     ap.add_argument("--workload", choices=["C2", "C3"], default=WORKLOAD,
-                    help="C2: 2,048 x 2,000 samples vs 1 Mb (default); C3: 8,192 uneven reads vs 5 Mb")
+                    help="C3: 8,192 uneven reads vs 5 Mb (default); C2: 2,048 x 2,000 samples vs 1 Mb")
+    ap.add_argument("--no-c2", action="store_true", help="do not add the C2 sub-record to a C3 line")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

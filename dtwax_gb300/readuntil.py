@@ -45,20 +45,25 @@ class ServeConfig:
     seed: int = 7
 
 
-def make_pool(genome: bytes, other: bytes, table, cfg: ServeConfig):
-    n = cfg.pool_reads
-    rng = np.random.default_rng(cfg.seed)
+def make_pool(genome: bytes, other: bytes, table, cfg: ServeConfig, held_out: bool = False, n: int = 0):
+    """Reads the simulated sequencer serves.  held_out=True draws a separate
+    set from the same generator with other seeds (for calibrating the accept /
+    reject rates on reads that are never served)."""
+    n = n or cfg.pool_reads
+    seed = cfg.seed + (1000 if held_out else 0)
+    rng = np.random.default_rng(seed)
     mask = (rng.random(n) < cfg.target_fraction).astype(np.int8)
     reads = synth.simulate_reads(genome, other, table, [cfg.chunk * cfg.chunks_per_read] * n, mask,
-                                 seed=cfg.seed + 1)
+                                 seed=seed + 1)
     return reads
 
 
 def calibrate(clf, reads, cfg: ServeConfig, n: int = 256):
-    """Per-sample accept / reject rates from the first chunk of n pool reads,
+    """Per-sample accept / reject rates from the first chunk of n reads,
     classified offline: accept below the lowest non-target rate, reject above
     the highest target rate (so one chunk decides every read the data
-    separates, and ambiguous reads get more chunks)."""
+    separates, and ambiguous reads get more chunks).  Pass reads that are not
+    served (make_pool(..., held_out=True)) for a held-out call accuracy."""
     n = min(n, reads.n)
     first = [reads.read(i)[: cfg.chunk] for i in range(n)]
     res = clf.classify(first)

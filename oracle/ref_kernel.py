@@ -30,6 +30,16 @@ queries are read up to index n_reads*2048 + 31 (the reference allocates the
 same 32-entry tail), reference tiles up to (REF_LEN/832)*832 - 1, the row
 state up to n_reads*REF_LEN - 1, and dist[block] per block.  The kernel has no
 waits and no data-dependent loop bounds.
+
+The row state is indexed as block_id * REF_LEN + column in 32-bit int
+(DTW.cu:208, :293, :325, :419-456, :546), which overflows once
+n_reads * REF_LEN passes 2^31 - 1: 2,147 reads per launch for the 1 Mb
+geometry, 429 for the 5 Mb one.  launch() refuses more reads per launch than
+that (max_reads_per_launch), so the kernel never indexes out of bounds.
+
+The reference's sources are found through the DTWAX_REFERENCE environment
+variable (the reference project's root); oracle/Makefile sets it.  Without it
+build() keeps the prebuilt cubins.
 """
 from __future__ import annotations
 
@@ -43,8 +53,13 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_ref")
 HARNESS = os.path.join(HERE, "ref_dtw_harness.cu")
-REFERENCE_ROOT = os.environ.get("DTWAX_REFERENCE", "/root/reference")
-REFERENCE_INCLUDE = os.path.join(REFERENCE_ROOT, "src", "include")
+INT32_MAX = 2 ** 31 - 1
+
+
+def reference_include():
+    """src/include of the reference project named by DTWAX_REFERENCE, or None."""
+    root = os.environ.get("DTWAX_REFERENCE")
+    return os.path.join(root, "src", "include") if root else None
 
 TILE = 832            # SEGMENT_SIZE 26 x WARP_SIZE 32 (common.hpp:88)
 QUERY_LEN = 2048      # common.hpp:58
@@ -62,6 +77,8 @@ GEOMETRIES = {
     "fp32_8320": ("fp32", 8320, False),          # 2 x 4,160 concatenated
     "fp32_94848": ("fp32", 94848, False),        # 2 x 47,424 concatenated (114 tiles)
     "fp32_2000128": ("fp32", 2000128, False),    # 2 x 1,000,064 concatenated: a 1 Mb genome (2,404 tiles)
+    "fp16_5000320": ("fp16", 5000320, False),    # 6,010 tiles: a 5 Mb genome (4,999,995 columns per strand)
+    "fp32_10000640": ("fp32", 10000640, False),  # 2 x 5,000,320 concatenated: a 5 Mb genome (12,020 tiles)
     "fp16_4160_rd": ("fp16", 4160, True),
     "fp16_48128_rd": ("fp16", 48128, True),
     "fp32_8320_rd": ("fp32", 8320, True),
@@ -84,14 +101,15 @@ def available(name: str) -> bool:
 
 
 def sources_present() -> bool:
-    return os.path.exists(os.path.join(REFERENCE_INCLUDE, "DTW.cu"))
+    inc = reference_include()
+    return bool(inc) and os.path.exists(os.path.join(inc, "DTW.cu"))
 
 
 def _compile(name: str) -> str:
     prec, ref_len, ref_del = GEOMETRIES[name]
     out = cubin_path(name)
     cmd = ["nvcc", "-cubin", "-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a",
-           f"-DHARNESS_REF_LEN={ref_len}", "-I", REFERENCE_INCLUDE]
+           f"-DHARNESS_REF_LEN={ref_len}", "-I", reference_include()]
     if not ref_del:
         cmd.append("-DNO_REF_DEL")
     if prec == "fp16":
@@ -244,11 +262,19 @@ class RefKernel:
         return torch.from_numpy(words.view(np.int32).copy()).cuda()
 
     # ---------------------------------------------------------- launches
+    def max_reads_per_launch(self) -> int:
+        """Most reads one launch may hold: the kernel's 32-bit row-state index
+        block_id * REF_LEN + column must stay below 2^31."""
+        return INT32_MAX // self.ref_len
+
     def launch(self, d_ref, d_query, d_dist, d_last, n_reads: int, first_read: int = 0, stream: int = 0):
         """One launch of FullDTW::DTW over reads [first_read, first_read + n_reads)
         of d_query; results to d_dist[0:n_reads], row state in d_last."""
         if n_reads <= 0:
             return
+        if n_reads > self.max_reads_per_launch():
+            raise ValueError(f"{n_reads} reads per launch overflow the kernel's 32-bit row-state index "
+                             f"(at most {self.max_reads_per_launch()} for REF_LEN {self.ref_len})")
         if d_ref.numel() < self.ref_len:
             raise ValueError("reference buffer too small")
         if d_query.numel() < (first_read + n_reads) * QUERY_LEN + 32:
@@ -276,6 +302,7 @@ class RefKernel:
         n = int(np.asarray(z).shape[0])
         d_q = self.queries(z)
         per = n if reads_per_launch <= 0 else min(reads_per_launch, n)
+        per = min(per, self.max_reads_per_launch())
         d_last = torch.empty(max(per, 1) * self.ref_len, dtype=torch.int32, device="cuda")
         d_dist = torch.empty(max(n, 1), dtype=torch.int32, device="cuda")
         stream = torch.cuda.current_stream().cuda_stream

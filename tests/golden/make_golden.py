@@ -162,4 +162,7 @@ def find_threshold_golden(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DTWAX_REFERENCE")
+    if not root:
+        sys.exit("usage: make_golden.py <root of the reference project> (or set DTWAX_REFERENCE)")
+    main(root)
