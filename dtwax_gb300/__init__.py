@@ -104,6 +104,7 @@ _SIGNATURES = {
     "dtwx_distances": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P, _P]),
     "dtwx_classify_device": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P, _P]),
     "dtwx_sync": (ctypes.c_int, [_P]),
+    "dtwx_normalize": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P, _I64P, _P]),
     "dtwx_debug_stall_next": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_uint32]),
     "dtwx_classify_plain_fp32": (ctypes.c_int, [_P, _P, _I64P, ctypes.c_int32, _P]),
     "dtwx_distances_static": (ctypes.c_int, [_P, ctypes.c_int64, _P, _I64P, ctypes.c_int32, ctypes.c_float, _P, _P]),
@@ -293,6 +294,16 @@ class Classifier:
         _check(self._lib.dtwx_classify_device(self._h, ctypes.c_void_p(d_raw), offsets.ctypes.data_as(_I64P),
                                               offsets.size - 1, ctypes.c_void_p(d_out), ctypes.c_void_p(stream)),
                self._h)
+
+    def normalize(self, d_raw: int, offsets: np.ndarray, d_query: int, stream: int = 0) -> np.ndarray:
+        """Window + z-score of device-resident raw samples into d_query
+        (normalizer::normalize); returns the output offsets (host)."""
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        out = np.zeros(offsets.size, np.int64)
+        _check(self._lib.dtwx_normalize(self._h, ctypes.c_void_p(d_raw), offsets.ctypes.data_as(_I64P),
+                                        offsets.size - 1, ctypes.c_void_p(d_query), out.ctypes.data_as(_I64P),
+                                        ctypes.c_void_p(stream)), self._h)
+        return out
 
     def sync(self):
         """Wait for the last device-pointer call (distances / classify_device)

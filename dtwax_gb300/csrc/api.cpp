@@ -976,6 +976,47 @@ int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets,
   return DTWX_OK;
 }
 
+int dtwx_normalize(dtwx_handle *h, const float *d_raw, const int64_t *offsets, int32_t n_reads, float *d_query,
+                   int64_t *out_offsets, void *stream) {
+  if (!h) return DTWX_E_ARG;
+  if (n_reads < 0 || (n_reads > 0 && (!d_raw || !offsets || !d_query)))
+    return fail(h, DTWX_E_ARG, "bad arguments");
+  for (int r = 0; r < n_reads; ++r)
+    if (offsets[r + 1] < offsets[r]) return fail(h, DTWX_E_ARG, "offsets must be non-decreasing");
+  CK(h, cudaSetDevice(h->device));
+  BatchCtx &c = h->ctx[0];
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const Windows w = make_windows(h->cfg, offsets, n_reads);
+  if (out_offsets) {
+    for (int r = 0; r < n_reads; ++r) out_offsets[r] = w.dst_off[r];
+    out_offsets[n_reads] = w.total;
+  }
+  if (n_reads == 0 || w.total == 0) return DTWX_OK;
+  const MetaLayout L = meta_layout(0, n_reads);
+  if (int rc = wait_meta(h, c)) return rc;
+  CK(h, c.h_meta.ensure(L.total));
+  CK(h, c.meta.ensure(L.total));
+  char *hm = c.h_meta.as<char>();
+  int32_t *len = reinterpret_cast<int32_t *>(hm + L.nsamp);
+  int64_t *src_off = reinterpret_cast<int64_t *>(hm + L.src_off);
+  int64_t *dst_off = reinterpret_cast<int64_t *>(hm + L.dst_off);
+  for (int r = 0; r < n_reads; ++r) {
+    len[r] = w.len[r];
+    src_off[r] = w.src_off[r];
+    dst_off[r] = w.dst_off[r];
+  }
+  CK(h, cudaMemcpyAsync(c.meta.p, c.h_meta.p, L.total, cudaMemcpyHostToDevice, st));
+  CK(h, cudaEventRecord(c.meta_free, st));
+  c.meta_pending = true;
+  const char *dm = c.meta.as<char>();
+  CK(h, launch_normalize(d_raw, 0, reinterpret_cast<const int64_t *>(dm + L.src_off),
+                         reinterpret_cast<const int64_t *>(dm + L.dst_off),
+                         reinterpret_cast<const int32_t *>(dm + L.nsamp), nullptr, nullptr, n_reads, h->cfg.norm_eps,
+                         d_query, st));
+  h->last_launches = 1;
+  return DTWX_OK;
+}
+
 int dtwx_sync(dtwx_handle *h) {
   if (!h) return DTWX_E_ARG;
   CK(h, cudaSetDevice(h->device));

@@ -196,6 +196,19 @@ int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets,
 int dtwx_classify_device(dtwx_handle *h, const float *d_raw, const int64_t *offsets,
                          int32_t n_reads, dtwx_result *d_out, void *stream);
 
+/* The window + z-score step alone, on device buffers: for read r the window
+ * of the handle's config (adapter_skip, query_len, require_full) of
+ * d_raw[offsets[r] .. offsets[r+1]) (FP32 samples on the device, offsets on
+ * the host) is z-scored per read, (x - mean) / sqrt(biased variance +
+ * norm_eps) with FP64 statistics, into d_query (device), windows back to back.
+ * out_offsets (host, n_reads + 1 entries, may be NULL) receives where each
+ * window starts in d_query and the total.  Asynchronous on `stream`.
+ * Replaces normalizer::normalize (src/include/normalizer.cu:71-113), which
+ * runs cudnnBatchNormalizationForwardTraining over reads x length samples in
+ * place (per read mean and biased variance, epsilon 1e-4). */
+int dtwx_normalize(dtwx_handle *h, const float *d_raw, const int64_t *offsets, int32_t n_reads,
+                   float *d_query, int64_t *out_offsets, void *stream);
+
 /* Wait for the kernels of the handle's most recent dtwx_distances or
  * dtwx_classify_device call and return their device-side status: DTWX_OK,
  * DTWX_E_TIMEOUT (a bounded wait gave up) or DTWX_E_CAPACITY (a task exceeded
