@@ -1,0 +1,109 @@
+"""Generate the FP64 answers of the precision-study (C2) and batched-uneven
+(C3) workloads for the GPU parity tests.
+
+The GPU tests regenerate the same seeded inputs with dtwax_gb300.synth and
+compare the library's results with the FP64 scores and end columns stored
+here, so the oracle does not have to run on the GPU host.  Inputs are checked
+first: each fixture stores SHA-256 digests of the raw samples and of the
+oracle's levels (rounded to FP32, the precision the library stores its
+reference in), and a test fails with a clear message if the generator gives
+different inputs on the machine it runs on.
+
+  python tests/golden/make_precision_fixtures.py [--only c2|c3] [--threads N]
+
+What is computed (the oracle's restatement of scripts/sdtw.py:86-116 and
+:205-225 and of load_reference.hpp:33-128, oracle/sdtw_oracle.c):
+  levels  = z-scored 6-mer levels of both strands, FP64, rounded to FP32;
+  queries = each read z-scored in FP64 with eps 1e-4 (normalizer.cu:397-399),
+            rounded to FP32 (the library's query buffer is FP32);
+  answers = FP64 sDTW of every query against each strand: the best score and
+            its end column per strand.
+
+C2: all 2,048 reads x 2,000 samples against the seeded 1 Mb genome
+    (8.19e12 cells; about 15 minutes on 8 x86 cores).
+C3: 48 of the 8,192 reads of U[1000, 8000] samples against the seeded 5 Mb
+    genome: the shortest and the longest read and 46 drawn with seed 7
+    (about 2e12 cells).
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+C2_PATH = os.path.join(HERE, "precision_c2.npz")
+C3_PATH = os.path.join(HERE, "uneven_c3.npz")
+C3_SAMPLE_SEED = 7
+C3_SAMPLE = 48
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def c3_sample(lengths: np.ndarray) -> np.ndarray:
+    """Indices of the C3 reads the fixture covers: shortest, longest, and a
+    seeded draw of the rest, in ascending order."""
+    rng = np.random.default_rng(C3_SAMPLE_SEED)
+    lo, hi = int(np.argmin(lengths)), int(np.argmax(lengths))
+    rest = np.setdiff1d(np.arange(lengths.size), [lo, hi])
+    pick = rng.choice(rest, C3_SAMPLE - 2, replace=False)
+    return np.sort(np.concatenate([[lo, hi], pick])).astype(np.int64)
+
+
+def oracle_inputs(O, w, idx):
+    """FP32-rounded oracle levels and z-scored queries of reads idx."""
+    fwd, rev = O.build_levels(w.genome, w.table.astype(np.float64))
+    fwd32, rev32 = fwd.astype(np.float32), rev.astype(np.float32)
+    qs, offs = [], [0]
+    for i in idx:
+        z = O.zscore(w.reads.read(int(i)).astype(np.float64), 1e-4).astype(np.float32)
+        qs.append(z)
+        offs.append(offs[-1] + z.size)
+    return fwd32, rev32, np.concatenate(qs), np.asarray(offs, np.int64)
+
+
+def make(name: str, threads: int):
+    from dtwax_gb300 import synth
+    from oracle import oracle as O
+
+    O.build()
+    w = synth.make_workload(name)
+    lengths = np.diff(w.reads.offsets)
+    idx = np.arange(w.reads.n, dtype=np.int64) if name == "C2" else c3_sample(lengths)
+    fwd32, rev32, q, offs = oracle_inputs(O, w, idx)
+    t = time.time()
+    sf, ef, sr, er = O.sdtw_batch(fwd32.astype(np.float64), rev32.astype(np.float64), q.astype(np.float64), offs,
+                                  n_threads=threads)
+    dt = time.time() - t
+    cells = float(lengths[idx].sum()) * fwd32.size * 2
+    print(f"{name}: {idx.size} reads, {cells:.3e} cells in {dt:.0f} s ({cells / dt / 1e9:.1f} GCUPS)", flush=True)
+    out = dict(read_index=idx, score_fwd=sf, end_fwd=ef, score_rev=sr, end_rev=er,
+               target=w.reads.target[idx], n_samples=lengths[idx].astype(np.int32),
+               ref_columns=np.int64(fwd32.size),
+               raw_sha256=np.array(sha(w.reads.raw)), levels_sha256=np.array(sha(np.stack([fwd32, rev32]))),
+               query_sha256=np.array(sha(q)), numpy_version=np.array(np.__version__))
+    np.savez_compressed(C2_PATH if name == "C2" else C3_PATH, **out)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", choices=["c2", "c3"])
+    ap.add_argument("--threads", type=int, default=0)
+    a = ap.parse_args()
+    for name in ("C3", "C2"):
+        if a.only and a.only != name.lower():
+            continue
+        make(name, a.threads)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,5 +1,9 @@
-"""Helpers shared by the GPU tests: classifiers on small seeded genomes and the
-oracle's answer for the same inputs."""
+"""Helpers shared by the GPU tests: classifiers on small seeded genomes, the
+oracle's answer for the same inputs, and the committed FP64 fixtures of the
+full-size workloads."""
+import hashlib
+import os
+
 import numpy as np
 
 from dtwax_gb300 import synth
@@ -42,3 +46,17 @@ def oracle_classify(oracle, clf, raw, offsets, eps=1e-4, query_len=0, skip=0):
 def reads_of_lengths(genome, other, table, lengths, seed=5):
     mask = np.arange(len(lengths)) % 2 == 0
     return synth.simulate_reads(genome, other, table, lengths, mask.astype(np.int8), seed=seed)
+
+
+def sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def load_fixture(path, workload):
+    """An FP64 fixture of tests/golden/make_precision_fixtures.py, after
+    checking that the seeded generator gives the same samples here."""
+    fx = dict(np.load(path))
+    assert sha(workload.reads.raw) == str(fx["raw_sha256"]), (
+        f"the seeded generator gave other samples here than where {os.path.basename(path)} was made "
+        f"(numpy {np.__version__} here, {fx['numpy_version']} there): regenerate the fixture")
+    return fx
