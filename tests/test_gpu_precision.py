@@ -1,74 +1,96 @@
-"""Precision study on the C2 generator (1 Mb genome): FP16 half2 cells with the
-per-strip running-minimum offset, MIXED (FP16 differences, FP32 path cost) and
-FP32 cells, each against the FP64 oracle.
+"""Precision study on the full C2 workload (2,048 reads x 2,000 samples against
+the seeded 1 Mb genome): FP16 half2 cells with the per-strip running-minimum
+offset, MIXED (FP16 differences, FP32 path cost) and FP32 cells, each against
+the FP64 oracle.
+
+The FP64 answers for all 2,048 reads are the committed fixture
+tests/golden/precision_c2.npz (tests/golden/make_precision_fixtures.py: the
+oracle's restatement of scripts/sdtw.py:86-116,205-225 on the same seeded
+inputs), so no oracle runs here; the inputs are checked against the
+fixture's digests first.
 
 Reported per precision: relative error of the best score (max, p99, median),
-exact end-position agreement, and agreement of the call at the threshold the
-FP64 scores give: the sweep of calc_classification_threshold.py, reported both
-with the reference's choice of the first best threshold (on the edge of the
-target scores when the classes separate) and with the centre of the
-best-accuracy plateau.  Targets: FP16 within 1e-2 relative, FP32 within 1e-5,
-MIXED within 1e-3, calls agree on >= 99.9 % of reads at the plateau centre.
-The FP64 oracle runs on a 256-read sample (5.1e11 cells on the host cores).
-Run with -s to see the table.
+exact end-position agreement, and agreement of the call at the threshold
+tuned on the FP64 scores.  The threshold rule is the reference tuner's own
+(src/ReadUntil/calc_classification_threshold.py:49-57): sweep 100,000
+thresholds over [0, max score] and keep the FIRST of maximal accuracy, target
+when score < threshold.  The >= 99.9 % agreement target is read against that
+rule.  The centre of the best-accuracy plateau is reported beside it.
+Targets: FP16 within 1e-2 relative, MIXED within 1e-3, FP32 within 1e-5;
+end columns of target reads within 2; FP32 end columns exact on >= 99.9 % of
+reads.  The fixture's inputs are the oracle's FP64 levels and z-scores
+rounded to FP32, while the library builds its reference and z-scores on the
+GPU, so the inputs can differ in the last bit; where two end columns of a
+read score within that rounding of each other the chosen one can differ (one
+read of 2,048 measured).  Run with -s to see the table.
 """
+import os
+
 import numpy as np
 import pytest
 
-from gpu_util import make_classifier, oracle_classify
+from conftest import GOLDEN
+from gpu_util import load_fixture, sha
 from dtwax_gb300 import synth, threshold
 
 pytestmark = pytest.mark.gpu
 
-N_READS = 256
+FIXTURE = os.path.join(GOLDEN, "precision_c2.npz")
+TOL = {"fp16": 1e-2, "mixed": 1e-3, "fp32": 1e-5}
 
 
 @pytest.fixture(scope="module")
 def study(built_lib, oracle):
-    w = synth.make_workload("C2", n_reads=N_READS)
+    import dtwax_gb300 as d
+    w = synth.make_workload("C2")
+    fx = load_fixture(FIXTURE, w)
+    fwd, rev = oracle.build_levels(w.genome, w.table.astype(np.float64))
+    assert sha(np.stack([fwd.astype(np.float32), rev.astype(np.float32)])) == str(fx["levels_sha256"])
+    assert (fx["read_index"] == np.arange(w.reads.n)).all()
     out = {}
-    for name, prec in (("fp16", 0), ("mixed", 2), ("fp32", 1)):
-        with make_classifier(w.genome, w.table, precision=prec) as clf:
+    for name, prec in (("fp16", d.FP16), ("mixed", d.MIXED), ("fp32", d.FP32)):
+        with d.Classifier(sequence=w.genome, level_table=w.table, precision=prec) as clf:
             out[name] = clf.classify(raw=w.reads.raw, offsets=w.reads.offsets)
-            if name == "fp32":
-                ora = oracle_classify(oracle, clf, w.reads.raw, w.reads.offsets)
-    sf, ef, sr, er = ora
-    score, end, strand = oracle.combine(sf, ef, sr, er)
-    t = w.reads.target == 1
+    score, end, strand = oracle.combine(fx["score_fwd"], fx["end_fwd"], fx["score_rev"], fx["end_rev"])
+    t = fx["target"] == 1
     th, acc = threshold.best_threshold(score[t], score[~t])
     thc, _ = threshold.best_threshold(score[t], score[~t], plateau="center")
-    return w, out, score, end, strand, (th, thc), acc
+    return w, fx, out, score, end, strand, (th, thc), acc
 
 
-def summarize(res, score, end, strand, ths):
+def summarize(res, fx, score, end, strand, ths):
     th, thc = ths
     rel = np.abs(res["score"] - score) / np.maximum(score, 1e-12)
+    rel_f = np.abs(res["score_fwd"] - fx["score_fwd"]) / np.maximum(fx["score_fwd"], 1e-12)
+    rel_r = np.abs(res["score_rev"] - fx["score_rev"]) / np.maximum(fx["score_rev"], 1e-12)
+    t = fx["target"] == 1
     return {
-        "max_rel": float(rel.max()), "p99_rel": float(np.percentile(rel, 99)),
+        "max_rel": float(max(rel.max(), rel_f.max(), rel_r.max())), "p99_rel": float(np.percentile(rel, 99)),
         "median_rel": float(np.median(rel)),
         "end_agree": float(((res["end_pos"] == end) & (res["strand"] == strand)).mean()),
-        "end_within_2": float(((np.abs(res["end_pos"] - end) <= 2) & (res["strand"] == strand)).mean()),
+        "end_within_2_targets": float(((np.abs(res["end_pos"] - end) <= 2) & (res["strand"] == strand))[t].mean()),
         "call_agree": float((threshold.call(res["score"], th) == threshold.call(score, th)).mean()),
         "call_agree_center": float((threshold.call(res["score"], thc) == threshold.call(score, thc)).mean()),
+        "call_disagree_reads": int((threshold.call(res["score"], th) != threshold.call(score, th)).sum()),
     }
 
 
 def test_precision_table(study, capsys):
-    w, out, score, end, strand, th, acc = study
-    rows = {k: summarize(v, score, end, strand, th) for k, v in out.items()}
+    w, fx, out, score, end, strand, th, acc = study
+    rows = {k: summarize(v, fx, score, end, strand, th) for k, v in out.items()}
     with capsys.disabled():
-        print(f"\nC2 precision study, {N_READS} reads x 2000 samples vs 2 x 999,995 columns; FP64 "
-              f"thresholds: first best {th[0]:.3f}, plateau centre {th[1]:.3f} ({acc:.2f} % accuracy)")
+        print(f"\nC2 precision study, all {w.reads.n} reads x 2000 samples vs 2 x {int(fx['ref_columns']):,} "
+              f"columns; FP64 thresholds (calc_classification_threshold.py rule): first best {th[0]:.3f} "
+              f"({acc:.2f} % accuracy), plateau centre {th[1]:.3f}")
         print(f"{'cells':6s} {'max rel':>10s} {'p99 rel':>10s} {'median rel':>11s} {'end exact':>10s} "
-              f"{'end +-2':>8s} {'call (first)':>13s} {'call (centre)':>14s}")
+              f"{'tgt end+-2':>10s} {'call (first)':>13s} {'flips':>6s} {'call (centre)':>14s}")
         for k, r in rows.items():
             print(f"{k:6s} {r['max_rel']:10.2e} {r['p99_rel']:10.2e} {r['median_rel']:11.2e} "
-                  f"{r['end_agree']:10.4f} {r['end_within_2']:8.4f} {r['call_agree']:13.4f} "
-                  f"{r['call_agree_center']:14.4f}")
-    assert rows["fp32"]["max_rel"] <= 1e-5
-    assert rows["fp16"]["max_rel"] <= 1e-2
-    assert rows["mixed"]["max_rel"] <= 1e-3
-    for k in ("fp16", "mixed", "fp32"):
-        assert rows[k]["call_agree_center"] >= 0.999
-    assert rows["fp32"]["call_agree"] >= 0.999
+                  f"{r['end_agree']:10.4f} {r['end_within_2_targets']:10.4f} {r['call_agree']:13.4f} "
+                  f"{r['call_disagree_reads']:6d} {r['call_agree_center']:14.4f}")
+    for k, r in rows.items():
+        assert r["max_rel"] <= TOL[k], (k, r["max_rel"])
+        assert r["call_agree"] >= 0.999, (k, r)          # the reference tuner's threshold rule
+        assert r["call_agree_center"] >= 0.999, (k, r)
+        assert r["end_within_2_targets"] == 1.0, (k, r)
     assert rows["fp32"]["end_agree"] >= 0.999
