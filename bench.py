@@ -449,11 +449,11 @@ def run_ours(args, rank, world, local):
     cells = w.cells()
     n_reads = w.reads.n
     peak = d.peak_probe(local, precision, 400.0)
-    use_graphs = 1 if (args.graphs or args.workload == "C3") else 0
+    use_graphs = 1 if (args.graphs or args.workload == "C3") and not args.no_graphs else 0
     clf = d.Classifier(sequence=w.genome, level_table=w.table, precision=precision, device=local,
                        cells_per_thread=args.cells, chunk_strips=args.strips, warps_per_cta=args.warps,
                        use_graphs=use_graphs, recurrence=d.REF_DEL if ref_del else d.NO_REF_DEL)
-    if args.autotune or args.workload == "C3":
+    if (args.autotune or args.workload == "C3") and not args.no_autotune:
         clf.autotune(n_reads, int(np.diff(w.reads.offsets).mean()))
     stream = torch.cuda.Stream()
     d_raw = torch.tensor(w.reads.raw, device="cuda")
@@ -634,6 +634,9 @@ def main():
     ap.add_argument("--warps", type=int, default=0, help="warps per CTA (0 = tuned)")
     ap.add_argument("--autotune", action="store_true", help="time candidate launch shapes before measuring")
     ap.add_argument("--graphs", action="store_true", help="replay the step as a captured CUDA graph")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="C3: keep the given or default launch shape (profiling a fixed launch)")
+    ap.add_argument("--no-graphs", action="store_true", help="C3: launch the kernels directly, no graph replay")
     ap.add_argument("--workload", choices=["C2", "C3"], default=WORKLOAD,
                     help="C3: 8,192 uneven reads vs 5 Mb (default); C2: 2,048 x 2,000 samples vs 1 Mb")
     ap.add_argument("--no-c2", action="store_true", help="do not add the C2 sub-record to a C3 line")

@@ -212,6 +212,14 @@ __device__ __forceinline__ void st_shared_if(uint32_t addr, uint32_t v, uint32_t
                : "memory");
 }
 
+// Drop one 128-byte L2 line without writing it back (PTX discard.global.L2,
+// sm_80 and later), issued by the lanes whose pred is set.  The contents of
+// the line become undefined; used on seam windows that have been consumed.
+__device__ __forceinline__ void discard_l2_if(const void *line, uint32_t pred) {
+  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %1, 0;\n\t@p discard.global.L2 [%0], 128;\n\t}" ::"l"(line),
+               "r"(pred));
+}
+
 __device__ __forceinline__ uint32_t ld_shared_u32(uint32_t addr) {
   uint32_t v;
   asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
@@ -846,6 +854,14 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(
         const int r = i0 + kWarp + lane;
         const float qn = r < n ? q[r] : 0.f;
         const V sn = (!first && r < rows) ? seam_in[r] : vinf;
+        // the previous window of the incoming seam (entries i0-32 .. i0-1,
+        // one aligned 128-byte line of this warp's scratch) was consumed in
+        // the previous 32 rows: drop it from L2 instead of letting it be
+        // written back to DRAM.  Only in the batched FP16 instance, where long
+        // reads make the seam columns outgrow L2 (the other instances'
+        // register allocation suffers from it)
+        if constexpr (PREC == 0 && !NH && !ST16)
+          discard_l2_if(seam_in + i0 - kWarp, is0 & (!first && i0 > 0 ? 1u : 0u));
         // the seam column leaving this strip is gathered in a register window
         // (lane l keeps row i0+l) and stored once per 32 rows, coalesced: no
         // lane-conditional store inside the row loop
