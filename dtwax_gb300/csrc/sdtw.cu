@@ -373,6 +373,11 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(
   static_assert(STRIP_BYTES % 1024 == 0, "strip tile must keep 1024-byte alignment");
   static_assert(S % 8 == 0, "row state and reference move in 16-byte groups");
   static_assert(!ST16 || PREC == 0, "the FP16 row state is built for FP16 cells");
+  // rows unrolled in the 32-row window loop, measured per cell type (C2 and
+  // the 5 Mb uneven batch): 8 gives MIXED cells +6 %; FP16 pairs are 2 %
+  // faster with 8 on 2,000-row reads but 0.6 % slower on the uneven batch,
+  // and FP32 cells do not change; 16 loses 13-17 % everywhere
+  constexpr int kRowUnroll = PREC == 2 ? 8 : 4;
 
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
@@ -625,7 +630,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(
         // lane-conditional store inside the row loop
         V sout = vinf;
         if (rows - i0 >= kWarp) {
-  #pragma unroll 4
+  #pragma unroll kRowUnroll
           for (int il = 0; il < kWarp; ++il) {
             row<SH, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
             if constexpr (SMEM_SEAM)
@@ -867,7 +872,7 @@ __global__ void __maxnreg__((sdtw_reg_cap<S, PREC>())) sdtw_kernel(
         // lane-conditional store inside the row loop
         V sout = vinf;
         if (rows - i0 >= kWarp) {
-#pragma unroll 4
+#pragma unroll kRowUnroll
           for (int il = 0; il < kWarp; ++il) {
             row<S, PREC>(D, R, P::qbcast(qwin, il), P::shfl(swin, il), m0);
             if constexpr (SMEM_SEAM)
