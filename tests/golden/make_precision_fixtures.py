@@ -24,6 +24,12 @@ C2: all 2,048 reads x 2,000 samples against the seeded 1 Mb genome
 C3: 48 of the 8,192 reads of U[1000, 8000] samples against the seeded 5 Mb
     genome: the shortest and the longest read and 46 drawn with seed 7
     (about 2e12 cells).
+C4: six reads served in 1,600-sample chunks against the seeded 5 Mb genome
+    of the Read Until simulation (3, 3, 3, 3, 2 and 1 chunks; targets and
+    non-targets): the best (score, end column, strand) after each chunk,
+    each chunk z-scored with its own statistics and resumed from the
+    previous chunk's last DP row in FP64, as the serving path does (one
+    process per read).
 """
 from __future__ import annotations
 
@@ -41,6 +47,11 @@ sys.path.insert(0, ROOT)
 
 C2_PATH = os.path.join(HERE, "precision_c2.npz")
 C3_PATH = os.path.join(HERE, "uneven_c3.npz")
+C4_PATH = os.path.join(HERE, "serving_c4.npz")
+C4_READ_SEED = 12
+C4_CHUNK = 1600
+C4_CHUNKS = [3, 3, 3, 3, 2, 1]
+C4_TARGET = [1, 0, 1, 0, 1, 0]
 C3_SAMPLE_SEED = 7
 C3_SAMPLE = 48
 
@@ -94,15 +105,63 @@ def make(name: str, threads: int):
     np.savez_compressed(C2_PATH if name == "C2" else C3_PATH, **out)
 
 
+def c4_reads():
+    """The C4 genome pair and the six served reads (seeded)."""
+    from dtwax_gb300 import synth
+    g = synth.random_genome(5_000_000, synth.GENOME_SEED)
+    o = synth.random_genome(5_000_000, synth.OTHER_SEED)
+    tab = synth.level_table()
+    reads = synth.simulate_reads(g, o, tab, [C4_CHUNK * k for k in C4_CHUNKS], C4_TARGET, seed=C4_READ_SEED)
+    return g, o, tab, reads
+
+
+def _c4_one(args):
+    """FP64 decisions after each chunk of one read (runs in its own process)."""
+    i, fwd32, rev32, x = args
+    from oracle import oracle as O
+    fwd, rev = fwd32.astype(np.float64), rev32.astype(np.float64)
+    rf = rr = None
+    out = []
+    for c in range(0, x.size, C4_CHUNK):
+        z = O.zscore(x[c:c + C4_CHUNK].astype(np.float64), 1e-4).astype(np.float32).astype(np.float64)
+        sf, ef, rf = O.sdtw(fwd, z, init_row=rf, want_row=True)
+        sr, er, rr = O.sdtw(rev, z, init_row=rr, want_row=True)
+        out.append((i, sf, ef, sr, er))
+    return out
+
+
+def make_c4():
+    import multiprocessing as mp
+    from oracle import oracle as O
+    O.build()
+    g, o, tab, reads = c4_reads()
+    fwd, rev = O.build_levels(g, tab.astype(np.float64))
+    fwd32, rev32 = fwd.astype(np.float32), rev.astype(np.float32)
+    t = time.time()
+    with mp.get_context("spawn").Pool(len(C4_CHUNKS)) as pool:
+        rows = pool.map(_c4_one, [(i, fwd32, rev32, reads.read(i)) for i in range(reads.n)])
+    print(f"C4: {reads.n} reads, {sum(C4_CHUNKS)} chunk-steps in {time.time() - t:.0f} s", flush=True)
+    flat = [r for per in rows for r in per]
+    np.savez_compressed(C4_PATH, read=np.array([r[0] for r in flat], np.int32),
+                        score_fwd=np.array([r[1] for r in flat]), end_fwd=np.array([r[2] for r in flat], np.int64),
+                        score_rev=np.array([r[3] for r in flat]), end_rev=np.array([r[4] for r in flat], np.int64),
+                        chunks=np.array(C4_CHUNKS, np.int32), target=np.array(C4_TARGET, np.int8),
+                        raw_sha256=np.array(sha(reads.raw)), levels_sha256=np.array(sha(np.stack([fwd32, rev32]))),
+                        numpy_version=np.array(np.__version__))
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["c2", "c3"])
+    ap.add_argument("--only", choices=["c2", "c3", "c4"])
     ap.add_argument("--threads", type=int, default=0)
     a = ap.parse_args()
-    for name in ("C3", "C2"):
+    for name in ("C4", "C3", "C2"):
         if a.only and a.only != name.lower():
             continue
-        make(name, a.threads)
+        if name == "C4":
+            make_c4()
+        else:
+            make(name, a.threads)
 
 
 if __name__ == "__main__":

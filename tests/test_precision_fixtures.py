@@ -49,3 +49,25 @@ def test_fixture_inputs_and_answers(oracle, name):
     np.testing.assert_array_equal(sr, fx["score_rev"][pos])
     np.testing.assert_array_equal(ef, fx["end_fwd"][pos])
     np.testing.assert_array_equal(er, fx["end_rev"][pos])
+
+
+def test_c4_serving_fixture_inputs(oracle):
+    """tests/golden/serving_c4.npz: the served reads and the 5 Mb levels are
+    still what the generator gives, and the fixture holds one decision per
+    chunk of every read."""
+    import hashlib
+    fx = dict(np.load(os.path.join(GOLDEN, "serving_c4.npz")))
+    chunks = [int(c) for c in fx["chunks"]]
+    g = synth.random_genome(5_000_000, synth.GENOME_SEED)
+    o = synth.random_genome(5_000_000, synth.OTHER_SEED)
+    tab = synth.level_table()
+    reads = synth.simulate_reads(g, o, tab, [1600 * k for k in chunks], fx["target"], seed=12)
+
+    def sha(a):
+        return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+    assert sha(reads.raw) == str(fx["raw_sha256"])
+    fwd, rev = oracle.build_levels(g, tab.astype(np.float64))
+    assert sha(np.stack([fwd.astype(np.float32), rev.astype(np.float32)])) == str(fx["levels_sha256"])
+    assert np.bincount(fx["read"]).tolist() == chunks
+    assert (np.diff(fx["score_fwd"][fx["read"] == 0]) > 0).all()  # the path cost grows chunk by chunk
