@@ -30,6 +30,8 @@ C4: six reads served in 1,600-sample chunks against the seeded 5 Mb genome
     each chunk z-scored with its own statistics and resumed from the
     previous chunk's last DP row in FP64, as the serving path does (one
     process per read).
+C5: the same for four reads (3, 3, 2, 1 chunks) against the seeded 12 Mb
+    genome of the memory-admitted stress run.
 """
 from __future__ import annotations
 
@@ -52,6 +54,9 @@ C4_READ_SEED = 12
 C4_CHUNK = 1600
 C4_CHUNKS = [3, 3, 3, 3, 2, 1]
 C4_TARGET = [1, 0, 1, 0, 1, 0]
+C5_PATH = os.path.join(HERE, "serving_c5.npz")
+C5_CHUNKS = [3, 3, 2, 1]
+C5_TARGET = [1, 0, 1, 0]
 C3_SAMPLE_SEED = 7
 C3_SAMPLE = 48
 
@@ -105,13 +110,13 @@ def make(name: str, threads: int):
     np.savez_compressed(C2_PATH if name == "C2" else C3_PATH, **out)
 
 
-def c4_reads():
-    """The C4 genome pair and the six served reads (seeded)."""
+def c4_reads(genome_len=5_000_000, chunks=C4_CHUNKS, target=C4_TARGET):
+    """The serving genome pair and the served reads (seeded)."""
     from dtwax_gb300 import synth
-    g = synth.random_genome(5_000_000, synth.GENOME_SEED)
-    o = synth.random_genome(5_000_000, synth.OTHER_SEED)
+    g = synth.random_genome(genome_len, synth.GENOME_SEED)
+    o = synth.random_genome(genome_len, synth.OTHER_SEED)
     tab = synth.level_table()
-    reads = synth.simulate_reads(g, o, tab, [C4_CHUNK * k for k in C4_CHUNKS], C4_TARGET, seed=C4_READ_SEED)
+    reads = synth.simulate_reads(g, o, tab, [C4_CHUNK * k for k in chunks], target, seed=C4_READ_SEED)
     return g, o, tab, reads
 
 
@@ -130,36 +135,41 @@ def _c4_one(args):
     return out
 
 
-def make_c4():
+def make_c4(name="C4"):
     import multiprocessing as mp
     from oracle import oracle as O
     O.build()
-    g, o, tab, reads = c4_reads()
+    if name == "C4":
+        path, chunks_, target_ = C4_PATH, C4_CHUNKS, C4_TARGET
+        g, o, tab, reads = c4_reads()
+    else:
+        path, chunks_, target_ = C5_PATH, C5_CHUNKS, C5_TARGET
+        g, o, tab, reads = c4_reads(12_000_000, C5_CHUNKS, C5_TARGET)
     fwd, rev = O.build_levels(g, tab.astype(np.float64))
     fwd32, rev32 = fwd.astype(np.float32), rev.astype(np.float32)
     t = time.time()
-    with mp.get_context("spawn").Pool(len(C4_CHUNKS)) as pool:
+    with mp.get_context("spawn").Pool(len(chunks_)) as pool:
         rows = pool.map(_c4_one, [(i, fwd32, rev32, reads.read(i)) for i in range(reads.n)])
-    print(f"C4: {reads.n} reads, {sum(C4_CHUNKS)} chunk-steps in {time.time() - t:.0f} s", flush=True)
+    print(f"{name}: {reads.n} reads, {sum(chunks_)} chunk-steps in {time.time() - t:.0f} s", flush=True)
     flat = [r for per in rows for r in per]
-    np.savez_compressed(C4_PATH, read=np.array([r[0] for r in flat], np.int32),
+    np.savez_compressed(path, read=np.array([r[0] for r in flat], np.int32),
                         score_fwd=np.array([r[1] for r in flat]), end_fwd=np.array([r[2] for r in flat], np.int64),
                         score_rev=np.array([r[3] for r in flat]), end_rev=np.array([r[4] for r in flat], np.int64),
-                        chunks=np.array(C4_CHUNKS, np.int32), target=np.array(C4_TARGET, np.int8),
+                        chunks=np.array(chunks_, np.int32), target=np.array(target_, np.int8),
                         raw_sha256=np.array(sha(reads.raw)), levels_sha256=np.array(sha(np.stack([fwd32, rev32]))),
                         numpy_version=np.array(np.__version__))
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["c2", "c3", "c4"])
+    ap.add_argument("--only", choices=["c2", "c3", "c4", "c5"])
     ap.add_argument("--threads", type=int, default=0)
     a = ap.parse_args()
-    for name in ("C4", "C3", "C2"):
+    for name in ("C5", "C4", "C3", "C2"):
         if a.only and a.only != name.lower():
             continue
-        if name == "C4":
-            make_c4()
+        if name in ("C4", "C5"):
+            make_c4(name)
         else:
             make(name, a.threads)
 

@@ -51,15 +51,16 @@ def test_fixture_inputs_and_answers(oracle, name):
     np.testing.assert_array_equal(er, fx["end_rev"][pos])
 
 
-def test_c4_serving_fixture_inputs(oracle):
-    """tests/golden/serving_c4.npz: the served reads and the 5 Mb levels are
-    still what the generator gives, and the fixture holds one decision per
-    chunk of every read."""
+@pytest.mark.parametrize("name,genome_len", [("c4", 5_000_000), ("c5", 12_000_000)])
+def test_serving_fixture_inputs(oracle, name, genome_len):
+    """tests/golden/serving_c4.npz and serving_c5.npz: the served reads and
+    the genome's levels are still what the generator gives, and the fixture
+    holds one decision per chunk of every read."""
     import hashlib
-    fx = dict(np.load(os.path.join(GOLDEN, "serving_c4.npz")))
+    fx = dict(np.load(os.path.join(GOLDEN, f"serving_{name}.npz")))
     chunks = [int(c) for c in fx["chunks"]]
-    g = synth.random_genome(5_000_000, synth.GENOME_SEED)
-    o = synth.random_genome(5_000_000, synth.OTHER_SEED)
+    g = synth.random_genome(genome_len, synth.GENOME_SEED)
+    o = synth.random_genome(genome_len, synth.OTHER_SEED)
     tab = synth.level_table()
     reads = synth.simulate_reads(g, o, tab, [1600 * k for k in chunks], fx["target"], seed=12)
 
