@@ -242,8 +242,12 @@ __device__ __forceinline__ __half2 rebase(float2 v, float2 dl) {
   return __floats2half2_rn(v.x + dl.x, v.y + dl.y);
 }
 
+// 128 registers: the kernel would take 165 (12 warps per SM); capped, a few
+// values spill outside the cell loop and 16 warps per SM hide more of the
+// cell chain's fixed latencies (measured on a 2,048-read batch: +6 % with
+// 4-warp CTAs, +10 % with 8-warp CTAs, the default for this kernel).
 template <int S>
-__global__ void __launch_bounds__(256, S <= 16 ? 2 : 1) sdtw_refdel_pairs_kernel(const SdtwParams p) {
+__global__ void __maxnreg__(128) sdtw_refdel_pairs_kernel(const SdtwParams p) {
   static_assert(S % 4 == 0, "row state moves in 16-byte groups");
   constexpr int W = kWarp * S;
   const int lane = threadIdx.x & 31;
