@@ -32,6 +32,8 @@ C4: six reads served in 1,600-sample chunks against the seeded 5 Mb genome
     process per read).
 C5: the same for four reads (3, 3, 2, 1 chunks) against the seeded 12 Mb
     genome of the memory-admitted stress run.
+C2R: the first 32 C2 reads with the REF_DEL recurrence (the left
+    predecessor of src/include/DTW.cu:23-29) against the 1 Mb genome.
 """
 from __future__ import annotations
 
@@ -55,6 +57,8 @@ C4_CHUNK = 1600
 C4_CHUNKS = [3, 3, 3, 3, 2, 1]
 C4_TARGET = [1, 0, 1, 0, 1, 0]
 C5_PATH = os.path.join(HERE, "serving_c5.npz")
+C2R_PATH = os.path.join(HERE, "refdel_c2.npz")
+C2R_READS = 32
 C5_CHUNKS = [3, 3, 2, 1]
 C5_TARGET = [1, 0, 1, 0]
 C3_SAMPLE_SEED = 7
@@ -92,13 +96,17 @@ def make(name: str, threads: int):
     from oracle import oracle as O
 
     O.build()
-    w = synth.make_workload(name)
+    ref_del = name == "C2R"
+    w = synth.make_workload("C2" if ref_del else name)
     lengths = np.diff(w.reads.offsets)
-    idx = np.arange(w.reads.n, dtype=np.int64) if name == "C2" else c3_sample(lengths)
+    if ref_del:
+        idx = np.arange(C2R_READS, dtype=np.int64)
+    else:
+        idx = np.arange(w.reads.n, dtype=np.int64) if name == "C2" else c3_sample(lengths)
     fwd32, rev32, q, offs = oracle_inputs(O, w, idx)
     t = time.time()
     sf, ef, sr, er = O.sdtw_batch(fwd32.astype(np.float64), rev32.astype(np.float64), q.astype(np.float64), offs,
-                                  n_threads=threads)
+                                  n_threads=threads, ref_del=ref_del)
     dt = time.time() - t
     cells = float(lengths[idx].sum()) * fwd32.size * 2
     print(f"{name}: {idx.size} reads, {cells:.3e} cells in {dt:.0f} s ({cells / dt / 1e9:.1f} GCUPS)", flush=True)
@@ -107,7 +115,7 @@ def make(name: str, threads: int):
                ref_columns=np.int64(fwd32.size),
                raw_sha256=np.array(sha(w.reads.raw)), levels_sha256=np.array(sha(np.stack([fwd32, rev32]))),
                query_sha256=np.array(sha(q)), numpy_version=np.array(np.__version__))
-    np.savez_compressed(C2_PATH if name == "C2" else C3_PATH, **out)
+    np.savez_compressed({"C2": C2_PATH, "C3": C3_PATH, "C2R": C2R_PATH}[name], **out)
 
 
 def c4_reads(genome_len=5_000_000, chunks=C4_CHUNKS, target=C4_TARGET):
@@ -162,10 +170,10 @@ def make_c4(name="C4"):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["c2", "c3", "c4", "c5"])
+    ap.add_argument("--only", choices=["c2", "c3", "c4", "c5", "c2r"])
     ap.add_argument("--threads", type=int, default=0)
     a = ap.parse_args()
-    for name in ("C5", "C4", "C3", "C2"):
+    for name in ("C2R", "C5", "C4", "C3", "C2"):
         if a.only and a.only != name.lower():
             continue
         if name in ("C4", "C5"):

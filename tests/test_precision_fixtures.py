@@ -1,8 +1,8 @@
 """The committed FP64 fixtures of the full-size workloads (no GPU).
 
-tests/golden/precision_c2.npz (all 2,048 C2 reads) and uneven_c3.npz (48 of
-the 8,192 C3 reads) hold the oracle's scores and end columns for seeded
-inputs; the GPU parity tests compare the library with them.  Checked here:
+tests/golden/precision_c2.npz (all 2,048 C2 reads), uneven_c3.npz (48 of
+the 8,192 C3 reads) and refdel_c2.npz (32 C2 reads, REF_DEL recurrence) hold
+the oracle's scores and end columns for seeded inputs; the GPU parity tests compare the library with them.  Checked here:
 the generator still gives the inputs the fixtures were made from (digests of
 the samples and of the FP32-rounded levels), and the oracle recomputes the
 stored answers of a few reads bit for bit.
@@ -15,17 +15,17 @@ import pytest
 from conftest import GOLDEN
 from dtwax_gb300 import synth
 
-FIXTURES = {"C2": "precision_c2.npz", "C3": "uneven_c3.npz"}
+FIXTURES = {"C2": "precision_c2.npz", "C3": "uneven_c3.npz", "C2R": "refdel_c2.npz"}
 
 
-@pytest.mark.parametrize("name", ["C2", "C3"])
+@pytest.mark.parametrize("name", ["C2", "C3", "C2R"])
 def test_fixture_inputs_and_answers(oracle, name):
     import hashlib
     path = os.path.join(GOLDEN, FIXTURES[name])
     if name == "C2" and not os.path.exists(path):
         pytest.skip("precision_c2.npz not generated yet")
     fx = dict(np.load(path))
-    w = synth.make_workload(name)
+    w = synth.make_workload("C2" if name == "C2R" else name)
 
     def sha(a):
         return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
@@ -44,7 +44,7 @@ def test_fixture_inputs_and_answers(oracle, name):
           for p in pos]
     offs = np.concatenate([[0], np.cumsum([q.size for q in qs])]).astype(np.int64)
     sf, ef, sr, er = oracle.sdtw_batch(fwd32.astype(np.float64), rev32.astype(np.float64),
-                                       np.concatenate(qs).astype(np.float64), offs)
+                                       np.concatenate(qs).astype(np.float64), offs, ref_del=name == "C2R")
     np.testing.assert_array_equal(sf, fx["score_fwd"][pos])
     np.testing.assert_array_equal(sr, fx["score_rev"][pos])
     np.testing.assert_array_equal(ef, fx["end_fwd"][pos])
