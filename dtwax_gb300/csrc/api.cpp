@@ -250,6 +250,24 @@ int log2_bucket(double x) { return x < 1.0 ? 0 : (int)std::floor(std::log2(x)); 
 // Launch shape of a sweep: user-fixed fields win, then an autotuned entry for
 // this (precision, batch size, read length) bucket, then the defaults; the
 // chunk width comes from the analytic model (times the tuned factor).
+// Largest CTA each sweep kernel launches with: the FP16-pair REF_DEL kernel is
+// capped at 128 registers, so 16 warps fill an SM's register file; the others
+// are compiled for at most 256 threads.
+int max_warps_per_cta(int precision, bool rd) { return rd && precision == 0 ? 16 : 8; }
+
+// Default warps per CTA of a REF_DEL sweep.  A REF_DEL work item is a whole
+// read (strand), so the batch alone sets the parallelism; the items are spread
+// evenly over the SMs, one CTA per SM.  Measured on the FP16-pair kernel with
+// 2,000-sample reads against 1 Mb: a warp takes 370 ms per read alone or 4 to
+// an SM, 487 ms 8 to an SM and 794 ms 16 to an SM, and 16 warps in one CTA
+// beat two 8-warp CTAs on the same SM (2,048 reads: 793 against 846 ms;
+// 4,096: 1,416 against 1,637 ms).  FP32 keeps 4-warp CTAs for large batches.
+int refdel_spread_warps(int precision, int64_t items, int sms) {
+  const int64_t per_sm = (std::max<int64_t>(items, 1) + sms - 1) / sms;
+  const int cap = precision == 0 ? max_warps_per_cta(precision, true) : 4;
+  return (int)std::min<int64_t>(per_sm, cap);
+}
+
 Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_rows) {
   Shape s;
   const Shape &f = h->fixed[precision];
@@ -263,10 +281,12 @@ Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_row
   const bool rd = h->cfg.recurrence == DTWX_REF_DEL;
   const int def_S = rd ? 32 : (precision == 2 ? 64 : 48);
   s.S = o.S ? o.S : (f.S ? f.S : (use_t ? t->second.S : def_S));
-  // 8-warp CTAs for the FP16-pair REF_DEL kernel (capped at 128 registers,
-  // 16 warps per SM; measured 4 % faster than 4-warp CTAs), else 4
-  const int def_warps = rd && precision == 0 ? 8 : 4;
-  s.warps = o.warps ? o.warps : (f.warps ? f.warps : (use_t ? t->second.warps : def_warps));
+  const int strands = precision == 0 ? 1 : (h->cfg.strand_mode == DTWX_STRANDS_CONCAT ? 1 : 2);
+  // warps per CTA: while tuning the candidate's (0 = the default below), else
+  // user-fixed, then autotuned, then the default
+  s.warps = o.S ? o.warps : (f.warps ? f.warps : (use_t ? t->second.warps : 0));
+  if (s.warps <= 0) s.warps = rd ? refdel_spread_warps(precision, n_tasks * strands, h->sms) : 4;
+  s.warps = std::min(s.warps, max_warps_per_cta(precision, rd));
   if (use_t && !f.G) g_scale = t->second.g_scale;
   if (o.S) g_scale = o.items > 0 ? o.items / 1000.0 : 1.0;  // candidate factor (per mille) while tuning
   int occ = sdtw_ctas_per_sm(precision, s.S, s.warps, rd);
@@ -274,7 +294,6 @@ Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_row
   const int W = kWarp * s.S;
   const int64_t strips = (h->m_cols + W - 1) / W;
   const int64_t total_warps = (int64_t)h->sms * occ * s.warps;
-  const int strands = precision == 0 ? 1 : (h->cfg.strand_mode == DTWX_STRANDS_CONCAT ? 1 : 2);
   if (rd) {
     s.G = (int)strips;  // REF_DEL: one chunk per task (a horizontal run crosses any chunk edge)
   } else if (f.G && !o.S) {
@@ -696,7 +715,8 @@ int create_common(const dtwx_config *cfg_in, const std::vector<double> &table, c
   if (cfg.cells_per_thread &&
       !sdtw_instance_exists(cfg.precision, cfg.cells_per_thread, cfg.recurrence == DTWX_REF_DEL))
     return fail(nullptr, DTWX_E_ARG, "cells_per_thread has no compiled kernel for this precision");
-  if (cfg.warps_per_cta < 0 || cfg.warps_per_cta > 8) return fail(nullptr, DTWX_E_ARG, "warps_per_cta must be 1..8");
+  if (cfg.warps_per_cta < 0 || cfg.warps_per_cta > max_warps_per_cta(cfg.precision, cfg.recurrence == DTWX_REF_DEL))
+    return fail(nullptr, DTWX_E_ARG, "warps_per_cta must be 1..8 (1..16 for FP16 REF_DEL cells)");
   if (cfg.chunk_strips < 0) return fail(nullptr, DTWX_E_ARG, "chunk_strips must be >= 0");
   const int64_t L = (int64_t)seq.size();
   if (L < kKmer) return fail(nullptr, DTWX_E_FORMAT, "reference shorter than one 6-mer");
@@ -1068,12 +1088,14 @@ int dtwx_autotune(dtwx_handle *h, int32_t n_reads_req, int32_t read_len, float *
   struct Cand { int S, warps, permille; };
   std::vector<Cand> cands;
   const bool rd = h->cfg.recurrence == DTWX_REF_DEL;
+  // warps 0: the default shape (for REF_DEL the batch spread evenly over the SMs)
   for (int si = 0; si < inst_count(prec); ++si)
-    for (int w : {4, 8})
+    for (int w : {0, 4, 8})
       for (int pm : {500, 1000, 2000}) {
         if (!sdtw_instance_exists(prec, inst_S(prec, si), rd)) continue;
         if (rd && pm != 1000) continue;  // one chunk per task: no chunk width to tune
-        if (!sdtw_ctas_per_sm(prec, inst_S(prec, si), w, rd)) continue;
+        if (w == 0 && !rd) continue;     // the default is 4 warps
+        if (w && !sdtw_ctas_per_sm(prec, inst_S(prec, si), w, rd)) continue;
         cands.push_back({inst_S(prec, si), w, pm});
       }
   float best = 1e30f;

@@ -245,7 +245,8 @@ __device__ __forceinline__ __half2 rebase(float2 v, float2 dl) {
 // 128 registers: the kernel would take 165 (12 warps per SM); capped, a few
 // values spill outside the cell loop and 16 warps per SM hide more of the
 // cell chain's fixed latencies (measured on a 2,048-read batch: +6 % with
-// 4-warp CTAs, +10 % with 8-warp CTAs, the default for this kernel).
+// 4-warp CTAs, +10 % with 8-warp CTAs).  With no launch bounds it takes up
+// to 16-warp CTAs, one per SM: the default spreads a batch that way.
 template <int S>
 __global__ void __maxnreg__(128) sdtw_refdel_pairs_kernel(const SdtwParams p) {
   static_assert(S % 4 == 0, "row state moves in 16-byte groups");

@@ -78,7 +78,8 @@ typedef struct dtwx_config {
   int32_t max_batch_reads; /* capacity hint for one classify call, 0 = grow on demand */
   int32_t cells_per_thread;/* DP columns per lane; 0 = autotune */
   int32_t chunk_strips;    /* strips (32 lanes x cells_per_thread columns) per work item; 0 = autotune */
-  int32_t warps_per_cta;   /* 0 = autotune */
+  int32_t warps_per_cta;   /* 1..8, 1..16 for FP16 REF_DEL cells; 0 = autotune, else 4, or for
+                              REF_DEL the batch spread evenly over the SMs (one CTA per SM) */
   int32_t use_graphs;      /* 1: dtwx_classify_device replays a captured CUDA graph when a batch
                               repeats (same buffers, offsets and stream): the first such batch runs
                               directly, the second is captured, later ones are replays */
@@ -270,8 +271,9 @@ int dtwx_last_sweep_ms(dtwx_handle *h, float *ms);
 
 /* Autotuner: time the sweep on a synthetic batch of n_reads reads of read_len
  * samples (cut to at most 2,048 reads and about 1.2e13 cells) for every
- * compiled cells-per-thread instance, 4 and 8 warps per CTA, and half / once /
- * twice the analytic chunk width; the fastest shape is used from then on for
+ * compiled cells-per-thread instance, 4 and 8 warps per CTA (and, for REF_DEL,
+ * the batch spread evenly over the SMs), and half / once / twice the analytic
+ * chunk width; the fastest shape is used from then on for
  * batches of n_reads reads of that length (log2 buckets of read count and
  * read length).  *best_ms gets its sweep time.  The reference fixes these at
  * compile time (SEGMENT_SIZE, BLOCK_NUM; src/include/common.hpp:64-79). */

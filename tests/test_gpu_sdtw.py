@@ -167,6 +167,32 @@ def test_ref_del_fp16_matches_oracle(lib, oracle, genome_pair):
             assert abs(int(res["end_pos"][i]) - int(best_end)) <= 2
 
 
+def test_ref_del_fp16_cta_shape_keeps_bits(lib, genome_pair):
+    """A REF_DEL warp sweeps its read alone, in the same order, whatever CTA it
+    sits in, so every CTA shape gives the same bits.  By default the reads are
+    spread evenly over the SMs: ceil(reads / SMs) warps per CTA (at most 16),
+    one CTA per SM."""
+    import torch
+    import dtwax_gb300 as d
+    g, o = genome_pair
+    tab = synth.level_table()
+    lengths = [2000, 1, 33, 1025, 2049, 3000, 500, 777] * 3
+    reads = reads_of_lengths(g, o, tab, lengths)
+    outs, shapes = [], []
+    for warps in (0, 1, 8, 16):
+        with make_classifier(g, tab, precision=d.FP16, recurrence=d.REF_DEL, warps_per_cta=warps) as clf:
+            outs.append(clf.classify(raw=reads.raw, offsets=reads.offsets))
+            shapes.append(clf.tuning())
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    n = len(lengths)
+    want = min(16, -(-n // sms))
+    assert shapes[0]["warps_per_cta"] == want and shapes[0]["ctas"] == -(-n // want)
+    assert [s["warps_per_cta"] for s in shapes[1:]] == [1, 8, 16]
+    for res in outs[1:]:
+        for k in ("score_fwd", "score_rev", "end_pos", "strand"):
+            np.testing.assert_array_equal(res[k], outs[0][k])
+
+
 def test_ref_del_rejects_other_cells(lib, genome_pair):
     import dtwax_gb300 as d
     g, _ = genome_pair

@@ -53,7 +53,10 @@ def test_config_combinations_are_checked(built_lib, kat, tmp_path):
            dict(precision=d.FP16, recurrence=d.REF_DEL, state_precision=d.STATE_FP16),
            dict(precision=d.MIXED, recurrence=d.REF_DEL),
            dict(precision=d.FP32, state_precision=d.STATE_FP16),
-           dict(precision=d.FP32, recurrence=d.REF_DEL, cells_per_thread=48)]
+           dict(precision=d.FP32, recurrence=d.REF_DEL, cells_per_thread=48),
+           # 16-warp CTAs only for the FP16-pair REF_DEL kernel (128 registers a thread)
+           dict(precision=d.FP16, warps_per_cta=16), dict(precision=d.FP32, recurrence=d.REF_DEL, warps_per_cta=16),
+           dict(precision=d.FP16, recurrence=d.REF_DEL, warps_per_cta=17), dict(warps_per_cta=-1)]
     for kw in bad:
         with pytest.raises(d.DtwxError) as e:
             d.Classifier(fasta=fasta, kmer_model=model, **kw)
