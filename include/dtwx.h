@@ -245,8 +245,7 @@ int dtwx_debug_stall_next(dtwx_handle *h, int32_t item, uint32_t spin_limit);
  * keeps until the process exits.  Limits: at most 4096 reads per call and 2048
  * samples per read; larger requests return DTWX_E_CAPACITY with a message in
  * dtwx_last_error(NULL).  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress); make that first call before any
- * stream capture.  All calls share the array, so calls that overlap on the GPU
+ * device address (cudaGetSymbolAddress).  All calls share the array, so calls that overlap on the GPU
  * (different streams, or several host threads) race and must be serialised by
  * the caller.  Asynchronous on `stream` (0 = legacy default stream).  A device
  * error of the call (a task the scratch cannot hold) marks every result with
