@@ -277,7 +277,7 @@ Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_row
   const bool use_t = t != h->tuned.end();
   // defaults measured on the 1 Mb / 2,048-read batch: 48 cells per lane (64 for
   // MIXED, whose reference takes half the registers) in 4-warp CTAs; the REF_DEL
-  // instances have 32 cells per lane (and 16 in FP32)
+  // kernels default to 32 cells per lane (FP32 cells also have a 16-cell instance)
   const bool rd = h->cfg.recurrence == DTWX_REF_DEL;
   const int def_S = rd ? 32 : (precision == 2 ? 64 : 48);
   s.S = o.S ? o.S : (f.S ? f.S : (use_t ? t->second.S : def_S));
