@@ -247,9 +247,6 @@ const void *ref_for(const dtwx_handle *h, int precision) {
 
 int log2_bucket(double x) { return x < 1.0 ? 0 : (int)std::floor(std::log2(x)); }
 
-// Launch shape of a sweep: user-fixed fields win, then an autotuned entry for
-// this (precision, batch size, read length) bucket, then the defaults; the
-// chunk width comes from the analytic model (times the tuned factor).
 // Largest CTA each sweep kernel launches with: the FP16-pair REF_DEL kernel is
 // capped at 128 registers, so 16 warps fill an SM's register file; the others
 // are compiled for at most 256 threads.
@@ -268,6 +265,9 @@ int refdel_spread_warps(int precision, int64_t items, int sms) {
   return (int)std::min<int64_t>(per_sm, cap);
 }
 
+// Launch shape of a sweep: user-fixed fields win, then an autotuned entry for
+// this (precision, batch size, read length) bucket, then the defaults; the
+// chunk width comes from the analytic model (times the tuned factor).
 Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_rows) {
   Shape s;
   const Shape &f = h->fixed[precision];
