@@ -39,7 +39,7 @@ struct Shape {
   int G = 0;      // strips per chunk
   int warps = 0;  // warps per CTA
   int grid = 0;   // CTAs
-  int items = 0;
+  int64_t items = 0;  // work items (while tuning: the candidate's chunk factor per mille)
   bool nh = false;  // narrow halo strips (FP16 pairs, narrow chunks)
 };
 
@@ -265,6 +265,13 @@ int refdel_spread_warps(int precision, int64_t items, int sms) {
   return (int)std::min<int64_t>(per_sm, cap);
 }
 
+// Rows a warp's seam buffers are sized for: the longest read rounded up to
+// 1,024 (at least 1,024), or -1 when the buffer offsets would leave int range.
+int seam_rows_capacity(int64_t max_rows) {
+  const int64_t cap = std::max<int64_t>(1024, (max_rows + 1023) / 1024 * 1024);
+  return cap + 64 > INT32_MAX / 8 ? -1 : (int)cap;
+}
+
 // Launch shape of a sweep: user-fixed fields win, then an autotuned entry for
 // this (precision, batch size, read length) bucket, then the defaults; the
 // chunk width comes from the analytic model (times the tuned factor).
@@ -310,7 +317,7 @@ Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_row
   const int64_t chunks = (strips + s.G - 1) / s.G;
   s.nh = precision == 0 && !rd && chunks > 1 && s.G <= kNarrowHaloMaxStrips && s.S % kNarrowHaloCells == 0;
   const int64_t items = n_tasks * chunks * strands;
-  s.items = (int)items;
+  s.items = items;
   const int64_t want = (items + s.warps - 1) / s.warps;
   s.grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)h->sms * occ, want));
   return s;
@@ -327,10 +334,13 @@ int enqueue_sweep(dtwx_handle *h, BatchCtx &c, int precision, cudaStream_t st, c
                   double mean_rows, int n_slots, const int32_t *d_nsamp, void *d_out,
                   float *state, bool finalize, int &launches) {
   Shape sh = pick_shape(h, precision, n_tasks, mean_rows);
+  // the work counter hands out 32-bit tickets, each warp one past the last item
+  if (sh.items + (int64_t)sh.grid * sh.warps >= INT32_MAX)
+    return fail(h, DTWX_E_CAPACITY, "batch has more work items than one sweep can number");
   h->last_shape[precision] = sh;
   const int pb = sdtw_pair_bytes(precision, h->cfg.recurrence == DTWX_REF_DEL);
-  int rows_cap = ((max_rows + 1023) / 1024) * 1024;
-  if (rows_cap < 1024) rows_cap = 1024;
+  const int rows_cap = seam_rows_capacity(max_rows);
+  if (rows_cap < 0) return fail(h, DTWX_E_CAPACITY, "read longer than a seam buffer can index");
   const int64_t per_warp = seam_bytes_per_warp(pb, rows_cap);
   const int64_t need = per_warp * (int64_t)sh.grid * sh.warps;
   const int strands = h->cfg.strand_mode == DTWX_STRANDS_CONCAT ? 1 : 2;
@@ -603,8 +613,8 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
                                nullptr, false, launches))
       return rc;
     const int pb = sdtw_pair_bytes(precision, h->cfg.recurrence == DTWX_REF_DEL);
-    int rows_cap = ((w.max_len + 1023) / 1024) * 1024;
-    if (rows_cap < 1024) rows_cap = 1024;
+    const int rows_cap = seam_rows_capacity(w.max_len);
+    if (rows_cap < 0) return fail(h, DTWX_E_CAPACITY, "read longer than a seam buffer can index");
     const int64_t per_warp = seam_bytes_per_warp(pb, rows_cap);
     int64_t seam_need = 0;
     for (int64_t t = 0; t < n_tasks; ++t) {
@@ -1142,7 +1152,7 @@ int dtwx_last_sweep_ms(dtwx_handle *h, float *ms) {
 int dtwx_get_tuning(const dtwx_handle *h, int32_t *out, int32_t n) {
   if (!h || !out || n < 0) return DTWX_E_ARG;
   const Shape &s = h->last_shape[h->cfg.precision];
-  const int32_t v[8] = {s.S, s.G, s.warps, s.grid, s.items,
+  const int32_t v[8] = {s.S, s.G, s.warps, s.grid, (int32_t)std::min<int64_t>(s.items, INT32_MAX),
                         s.S ? sdtw_ctas_per_sm(h->cfg.precision, s.S, s.warps,
                                                h->cfg.recurrence == DTWX_REF_DEL)
                             : 0,
