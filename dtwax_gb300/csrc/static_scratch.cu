@@ -81,6 +81,8 @@ extern "C" int dtwx_distances_static(const void *d_ref_pairs, int64_t ref_len, c
                                      dtwx_result *d_out, void *stream) {
   if (n_reads < 0 || ref_len <= 0 || !offsets || (n_reads > 0 && (!d_ref_pairs || !d_query || !d_out)))
     return st_fail(DTWX_E_ARG, "dtwx_distances_static: bad arguments");
+  if (n_reads > 0 && offsets[0] < 0)
+    return st_fail(DTWX_E_ARG, "dtwx_distances_static: offsets must start at 0 or later");
   if ((reinterpret_cast<uintptr_t>(d_ref_pairs) & 15) != 0)
     return st_fail(DTWX_E_ARG, "dtwx_distances_static: d_ref_pairs must be 16-byte aligned");
   if ((reinterpret_cast<uintptr_t>(d_out) & 7) != 0)
