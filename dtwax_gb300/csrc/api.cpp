@@ -490,6 +490,7 @@ int classify_common(dtwx_handle *h, const void *raw_host, const void *raw_dev, i
                     bool use_given_stream, int precision, bool one_launch_per_read) {
   if (!h) return fail(nullptr, DTWX_E_ARG, "null handle");
   if (n_reads < 0 || (n_reads > 0 && !offsets)) return fail(h, DTWX_E_ARG, "bad read batch");
+  if (n_reads > 0 && offsets[0] < 0) return fail(h, DTWX_E_ARG, "offsets must start at 0 or later");
   for (int r = 0; r < n_reads; ++r)
     if (offsets[r + 1] < offsets[r]) return fail(h, DTWX_E_ARG, "offsets must be non-decreasing");
   CK(h, cudaSetDevice(h->device));
@@ -964,6 +965,7 @@ int dtwx_distances(dtwx_handle *h, const float *d_query, const int64_t *offsets,
   if (!h) return DTWX_E_ARG;
   if (n_reads < 0 || (n_reads > 0 && (!d_query || !offsets || !d_out)))
     return fail(h, DTWX_E_ARG, "bad arguments");
+  if (n_reads > 0 && offsets[0] < 0) return fail(h, DTWX_E_ARG, "offsets must start at 0 or later");
   CK(h, cudaSetDevice(h->device));
   BatchCtx &c = h->ctx[0];
   cudaStream_t st = static_cast<cudaStream_t>(stream);  // 0 = the legacy default stream
@@ -1014,6 +1016,7 @@ int dtwx_normalize(dtwx_handle *h, const float *d_raw, const int64_t *offsets, i
   if (!h) return DTWX_E_ARG;
   if (n_reads < 0 || (n_reads > 0 && (!d_raw || !offsets || !d_query)))
     return fail(h, DTWX_E_ARG, "bad arguments");
+  if (n_reads > 0 && offsets[0] < 0) return fail(h, DTWX_E_ARG, "offsets must start at 0 or later");
   for (int r = 0; r < n_reads; ++r)
     if (offsets[r + 1] < offsets[r]) return fail(h, DTWX_E_ARG, "offsets must be non-decreasing");
   CK(h, cudaSetDevice(h->device));

@@ -160,7 +160,11 @@ int64_t dtwx_ref_len(const dtwx_handle *h);
  * dtwx_ref_len() floats.  For checking the reference builder. */
 int dtwx_get_reference(dtwx_handle *h, float *fwd, float *rev);
 
-/* Classify reads given as raw FP32 samples on the host: read r is
+/* Offsets (all entry points): n_reads + 1 host int64 values, non-decreasing
+ * and starting at 0 or later; anything else returns DTWX_E_ARG before any
+ * device work.
+ *
+ * Classify reads given as raw FP32 samples on the host: read r is
  * raw[offsets[r] .. offsets[r+1]).  Window, z-score (FP64 statistics),
  * sDTW of both strands and the min/argmin all run on the GPU; out[n_reads] is
  * written on return.  Replaces the batch loop of src/main.cu:217-271

@@ -101,3 +101,29 @@ def test_device_entries_mark_results_and_sync_reports(case, entry):
         again = run()
         clf.sync()
         _same(again, want)
+
+
+def test_offsets_before_the_buffer_are_refused(case):
+    """A negative first offset would start a read before the caller's buffer:
+    every handle entry point refuses it with DTWX_E_ARG before any device
+    work, and the handle keeps working."""
+    import torch
+    import dtwax_gb300 as d
+    genome, table, reads = case
+    bad = reads.offsets - 5
+    with make_classifier(genome, table, precision=d.FP16) as clf:
+        want = clf.classify(raw=reads.raw, offsets=reads.offsets)
+        d_raw = torch.tensor(reads.raw, dtype=torch.float32, device="cuda")
+        d_q = torch.zeros(reads.raw.size, dtype=torch.float32, device="cuda")
+        d_out = torch.zeros(32 * reads.n, dtype=torch.uint8, device="cuda")
+        calls = {"classify": lambda: clf.classify(raw=reads.raw, offsets=bad),
+                 "classify_device": lambda: clf.classify_device(d_raw.data_ptr(), bad, d_out.data_ptr()),
+                 "distances": lambda: clf.distances(d_q.data_ptr(), bad, d_out.data_ptr()),
+                 "normalize": lambda: clf.normalize(d_raw.data_ptr(), bad, d_q.data_ptr())}
+        for name, call in calls.items():
+            with pytest.raises(d.DtwxError) as ei:
+                call()
+            assert ei.value.code == -1, name
+            assert "start at 0" in str(ei.value), name
+        torch.cuda.synchronize()
+        _same(clf.classify(raw=reads.raw, offsets=reads.offsets), want)

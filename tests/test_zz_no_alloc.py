@@ -120,4 +120,10 @@ def test_static_scratch_refuses_oversized_requests(built_lib):
                                    ctypes.c_void_p(d_out.data_ptr()), None)
     assert rc == -1  # DTWX_E_ARG: the reference pairs are read in 16-byte loads
     assert b"16-byte" in lib.dtwx_last_error(None)
+
+    before = np.array([-5, 100], np.int64)  # would start the read before d_query
+    rc = lib.dtwx_distances_static(ctypes.c_void_p(d_ref.data_ptr()), 1000, ctypes.c_void_p(d_q.data_ptr()),
+                                   before.ctypes.data_as(i64p), 1, ctypes.c_float(1.0),
+                                   ctypes.c_void_p(d_out.data_ptr()), None)
+    assert rc == -1 and b"start at 0" in lib.dtwx_last_error(None)
     torch.cuda.synchronize()
