@@ -317,6 +317,18 @@ Shape pick_shape(dtwx_handle *h, int precision, int64_t n_tasks, double mean_row
   const int64_t chunks = (strips + s.G - 1) / s.G;
   s.nh = precision == 0 && !rd && chunks > 1 && s.G <= kNarrowHaloMaxStrips && s.S % kNarrowHaloCells == 0;
   const int64_t items = n_tasks * chunks * strands;
+  // FP16 pairs, default shape, a batch of several waves: the SM's warps in one
+  // CTA instead of occ 4-warp CTAs (the same warps per SM, so the same chunks
+  // and bits).  Measured on the 2,048-read / 1 Mb batch at 48 cells per lane:
+  // 487 against 501 ms; equal on the 8,192-read / 5 Mb one.  Single-wave
+  // batches (serving) keep 4-warp CTAs, which leave room for the next batch.
+  if (!rd && precision == 0 && !o.S && !f.warps && !use_t && items >= 2 * total_warps && occ > 1) {
+    const int full = occ * s.warps;
+    if (sdtw_ctas_per_sm(precision, s.S, full, false) == 1) {
+      s.warps = full;
+      occ = 1;
+    }
+  }
   s.items = items;
   const int64_t want = (items + s.warps - 1) / s.warps;
   s.grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)h->sms * occ, want));
